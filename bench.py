@@ -1,0 +1,398 @@
+"""Benchmark: 30-qubit complex128 forward (gate applies/s) on one GB300.
+
+Workload (the forward that the headline metric is quoted on): 30 qubits,
+complex128 (17.2 GB statevector), Hadamard on every qubit then 20 layers of
+[RX, RY, RZ on every qubit; CNOT i->i+1], angles uniform [0, 2pi) from seed
+1: 2410 gates, fusion windows on. A step is one reset to |0...0> plus the
+forward of all 2410 gates with the state resident in HBM; `value` = gates /
+step time (CUDA events on the library's stream, max over ranks). The state
+(17.2 GB) is larger than L2 (129 MB), so no flush is needed between steps.
+
+`e2e` runs the same forward through the Circuit API with host buffers: per
+step the parameters are set from a pinned host array (the gate list is
+uploaded), the forward runs, and the whole statevector comes back to pinned
+host memory as split real/imaginary arrays (the reference's
+retrieve_amplitudes_on_host layout, which its forward() performs every call).
+
+`adjoint` reports the adjoint-gradient part of the metric on the 24-qubit,
+1152-parameter ring ansatz (loss sum_q w_q <Z_q>, params seed 2, weights
+seed 3): adjoint grads/s, and parameter shift timed on a sample of the
+parameters through the same GPU kernels.
+
+`--impl reference` times the CPU oracle (a C/OpenMP restatement of the
+reference's multithreading path) on the host cores on a bounded sample of the
+same workload. Under torchrun every rank runs an independent replica
+(the path does not shard on one node here); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "30-qubit gate applies/s + HBM GB/s; adjoint vs param-shift grads/s at 1e-10"
+UNIT = "gate-applies/s"
+# FP64 multiply-add throughput of a GB300 measured with an independent-FMA-chain kernel
+# (0.504 T FMA/s = 1.0 TFLOP/s); complex128 arithmetic is bounded by it.
+FP64_FMA_PEAK_T = 0.504
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ reference
+def run_reference(args, world, rank):
+    """CPU oracle (port of the reference's multithreading path) on the host cores."""
+    if rank != 0:
+        return None
+    from damavand_gb300.workloads import count, ladder_circuit
+    from oracle import oracle
+    oracle.build()
+    n = args.qubits
+    gates = [g for g in ladder_circuit(n, args.layers, seed=1) if not g[3]]
+    state = oracle.zero_state(n)
+    per_step = args.ref_gates
+    pos = 0
+
+    def step():
+        nonlocal pos, state
+        sel = [gates[(pos + i) % len(gates)] for i in range(per_step)]
+        pos += per_step
+        t0 = time.perf_counter()
+        oracle.forward(n, sel, state)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(args.steps)]
+    total = sum(times)
+    value = per_step * args.steps / total
+    threads = oracle.num_threads()
+    sample = (f"{per_step} consecutive gates of the {count(gates)}-gate {n}-qubit forward per step "
+              f"(clone + per-amplitude update per gate, as the reference does)")
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic",
+        "impl": "reference",
+        "config": workload_config(args, count(gates)),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def workload_config(args, gates):
+    return {"workload": f"{args.qubits}-qubit complex128 forward: H on all qubits + {args.layers} x "
+                        f"[RX,RY,RZ per qubit; CNOT i->i+1], angles U[0,2pi) seed 1",
+            "qubits": args.qubits, "gates": gates, "layers": args.layers, "precision": "complex128",
+            "fusion": "qubit windows" if not args.no_fusion else "none",
+            "l2": "inputs larger than L2 (statevector 2^n x 16 B), no flush", "parallelism": "replicas"}
+
+
+# ------------------------------------------------------------------------ ours
+def cpu_baseline(args):
+    """Times the oracle on a bounded sample at the bench's size on the host cores."""
+    from damavand_gb300.workloads import ladder_circuit
+    from oracle import oracle
+    oracle.build()
+    n = args.qubits
+    gates = [g for g in ladder_circuit(n, args.layers, seed=1) if not g[3]]
+    state = oracle.zero_state(n)
+    done, t0 = 0, time.perf_counter()
+    while done < len(gates) and (time.perf_counter() - t0) < args.cpu_seconds:
+        oracle.forward(n, [gates[done]], state)
+        done += 1
+    el = time.perf_counter() - t0
+    del state
+    return {"value": done / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"first {done} gates of the {len(gates)}-gate {n}-qubit forward ({el:.1f} s)"}
+
+
+def adjoint_section(args):
+    from damavand_gb300 import Circuit
+    from damavand_gb300._lib import KERNEL_ADJOINT
+    from damavand_gb300.workloads import add_to_circuit, loss_weights, parameters, ring_ansatz
+    n, layers = 24, 16
+    gates = ring_ansatz(n, layers, seed=2)
+    w = loss_weights(n, 3)
+    p = parameters(gates)
+    c = Circuit(n)
+    add_to_circuit(c, gates)
+    c.adjoint_gradient(w)  # warm-up
+    t0 = time.perf_counter()
+    reps = 2
+    for _ in range(reps):
+        loss, g = c.adjoint_gradient(w)
+    t_adj = (time.perf_counter() - t0) / reps
+    # parameter shift on the same GPU kernels, on a sample of parameters
+    k = min(args.ps_params, p.size)
+    idx = np.linspace(0, p.size - 1, k).astype(int)
+    ps = np.empty(k)
+    t0 = time.perf_counter()
+    for j, i in enumerate(idx):
+        up, dn = p.copy(), p.copy()
+        up[i] += math.pi / 2
+        dn[i] -= math.pi / 2
+        c.set_parameters(up)
+        lu = c.loss(w)
+        c.set_parameters(dn)
+        ld = c.loss(w)
+        ps[j] = 0.5 * (lu - ld)
+    t_ps_per_param = (time.perf_counter() - t0) / k
+    c.set_parameters(p)
+    t_ps = t_ps_per_param * p.size
+    return {"qubits": n, "params": int(p.size), "gates": len(gates), "adjoint_s": t_adj,
+            "adjoint_grads_per_s": p.size / t_adj, "param_shift_s_extrapolated": t_ps,
+            "param_shift_grads_per_s": p.size / t_ps, "param_shift_sampled_params": int(k),
+            "speedup_vs_param_shift": t_ps / t_adj, "max_abs_diff_vs_param_shift": float(np.max(np.abs(g[idx] - ps))),
+            "loss": loss}
+
+
+def run_ours(args, world, rank, local):
+    import ctypes
+
+    from damavand_gb300 import Circuit
+    from damavand_gb300._lib import (KERNEL_ADJOINT, KERNEL_REDUCE, KERNEL_SINGLE, KERNEL_WINDOW, check, dptr, lib)
+    from damavand_gb300.workloads import add_to_circuit, count, ladder_circuit, parameters
+
+    check(lib.dmv_set_device(local))
+    n = args.qubits
+    gates = ladder_circuit(n, args.layers, seed=1)
+    G = count(gates)
+    c = Circuit(n, "gpu", fusion=not args.no_fusion)
+    add_to_circuit(c, gates)
+    st = c.state()
+    S = (1 << n) * 16
+
+    def step():
+        c.reset_amplitudes()
+        c.forward()
+
+    for _ in range(args.warmup):
+        step()
+    st.synchronize()
+    passes, fused_ops, bytes_moved = c.plan_stats()
+
+    # ---- timed region: device-resident forward, CUDA events on the library's stream
+    barrier(world)
+    st.synchronize()
+    lib.dmv_profile_reset()
+    lib.dmv_profile_enable(1)
+    launches0 = lib.dmv_kernel_launch_count()
+    with ClockSampler(local) as clocks:
+        check(lib.dmv_state_event_begin(st.handle))
+        for _ in range(args.steps):
+            step()
+        ms = ctypes.c_double()
+        check(lib.dmv_state_event_end(st.handle, ctypes.byref(ms)))
+    launches = lib.dmv_kernel_launch_count() - launches0
+    lib.dmv_profile_enable(0)
+    barrier(world)
+    step_ms = max_over_ranks(world, ms.value / args.steps)
+    value = world * G / (step_ms / 1e3)
+
+    fam = {}
+    for name, f in (("window", KERNEL_WINDOW), ("single", KERNEL_SINGLE), ("reduce", KERNEL_REDUCE),
+                    ("adjoint", KERNEL_ADJOINT)):
+        l, t, b, fm = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib.dmv_profile_read(f, ctypes.byref(l), ctypes.byref(t), ctypes.byref(b), ctypes.byref(fm)))
+        fam[name] = {"launches": l.value, "ms": t.value, "bytes": b.value, "fp64_fma": fm.value}
+    dom = max(fam, key=lambda k: fam[k]["ms"])
+    d = fam[dom]
+    peak, peak_kind = load_peaks()
+    per_launch_bytes = d["bytes"] / max(d["launches"], 1)
+    avg_launch_s = d["ms"] / max(d["launches"], 1) / 1e3
+    achieved = per_launch_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
+    traffic = None
+    prof_path = os.path.join(REPO, "profiles", "traffic_per_launch.json")
+    if os.path.exists(prof_path):
+        try:
+            traffic = json.load(open(prof_path)).get(f"{dom}_n{n}")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": f"k_apply_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_launch_s * 1e3}
+    # The same kernel against the FP64 multiply-add ceiling it actually meets on GB300.
+    fp64_rate = d["fp64_fma"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else 0.0
+    roofline_fp64 = {"bound": "fp64", "achieved": fp64_rate, "peak": FP64_FMA_PEAK_T, "unit": "T FMA/s",
+                     "frac": fp64_rate / FP64_FMA_PEAK_T,
+                     "peak_source": "measured (FP64 FMA chain kernel on this pool's GB300, 0.504 T FMA/s)"}
+    total_pass_bytes = sum(v["bytes"] for v in fam.values())
+    total_kernel_ms = sum(v["ms"] for v in fam.values())
+
+    # ---- e2e through the Circuit API with pinned host buffers
+    params = parameters(gates)
+    pin_params = np.ascontiguousarray(params)
+    re = np.empty(1 << n)
+    im = np.empty(1 << n)
+    registered = []
+    for a in (pin_params, re, im):
+        if lib.dmv_host_register(a.ctypes.data, a.nbytes) == 0:
+            registered.append(a)
+    h2d = pin_params.nbytes + G * ctypes.sizeof(ctypes.c_double) * 12  # parameters + uploaded op list
+    d2h = re.nbytes + im.nbytes
+    for _ in range(1):
+        c.set_parameters(pin_params)
+        step()
+        check(lib.dmv_state_copy_to_host(st.handle, dptr(re), dptr(im)))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c.set_parameters(pin_params)
+        step()
+        check(lib.dmv_state_copy_to_host(st.handle, dptr(re), dptr(im)))
+    e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / args.steps)
+    for a in registered:
+        lib.dmv_host_unregister(a.ctypes.data)
+    del re, im
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic (seeded angles, seed 1)",
+        "config": workload_config(args, G),
+        "hbm_gbs_pass_bytes": total_pass_bytes / (total_kernel_ms / 1e3) / 1e9 if total_kernel_ms else None,
+        "per_gate_equiv_gbs": G * 2 * S * args.steps / (ms.value / 1e3) / 1e9,
+        "plan": {"passes": passes, "fused_ops": fused_ops, "bytes_per_forward": bytes_moved},
+        "kernels": fam,
+        "roofline": roofline,
+        "roofline_fp64": roofline_fp64,
+        "e2e": {"value": world * G / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_adjoint:
+        out["adjoint"] = adjoint_section(args)
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--layers", type=int, default=20)
+    ap.add_argument("--no-fusion", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-gates", type=int, default=3, help="gates per reference step")
+    ap.add_argument("--ps-params", type=int, default=8, help="parameters sampled for parameter shift")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+    else:
+        out = run_ours(args, world, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

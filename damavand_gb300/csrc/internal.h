@@ -1,0 +1,181 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/damavand_gpu.h"
+
+namespace dmv {
+
+// ---------------------------------------------------------------------------
+// Error reporting: every entry point returns a status and records the last
+// error (thread-local) with a message. Nothing calls exit().
+// ---------------------------------------------------------------------------
+int set_error(int code, const char* fmt, ...);
+void clear_error();
+int last_error();
+
+#define DMV_CUDA_TRY(expr)                                                           \
+  do {                                                                               \
+    cudaError_t dmv_e_ = (expr);                                                     \
+    if (dmv_e_ != cudaSuccess) {                                                     \
+      return ::dmv::set_error(dmv_e_ == cudaErrorMemoryAllocation ? DMV_ERR_OOM      \
+                                                                  : DMV_ERR_CUDA,    \
+                              "%s failed: %s (%s:%d)", #expr,                        \
+                              cudaGetErrorString(dmv_e_), __FILE__, __LINE__);       \
+    }                                                                                \
+  } while (0)
+
+#define DMV_TRY(expr)                       \
+  do {                                      \
+    int dmv_rc_ = (expr);                   \
+    if (dmv_rc_ != DMV_OK) return dmv_rc_;  \
+  } while (0)
+
+// Counts the library's own kernel launches (reported by the benchmark).
+void count_launch(int64_t n = 1);
+
+// Optional per-launch CUDA-event profiling (dmv_profile_*). prof_begin
+// returns a token (or -1 when profiling is off); prof_end closes it.
+int64_t prof_begin(int family, cudaStream_t stream, double algorithmic_bytes, double multiply_adds = 0.0);
+void prof_end(int64_t token, cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Gate matrices and fused-op encoding
+// ---------------------------------------------------------------------------
+// Op arithmetic classes: the kernels specialise on them to spend as few
+// FP64 operations as the matrix allows (FP64 is ~1/70 of FP32 on GB300).
+enum OpClass : int32_t {
+  OP_GENERAL = 0,  // full complex 2x2
+  OP_DIAG = 1,     // m01 = m10 = 0
+  OP_SWAP = 2,     // exactly [[0,1],[1,0]] (X, CNOT): a pure exchange
+  OP_REAL = 3,     // all four entries real
+  OP_ANTI = 4      // m00 = m11 = 0 (Y and scaled exchanges)
+};
+
+// Control kinds inside a fused pass.
+enum CtrlKind : int32_t {
+  CTRL_NONE = 0,
+  CTRL_LOCAL = 1,   // control qubit is one of the pass's local bits
+  CTRL_GLOBAL = 2   // control qubit is outside the tile: constant per tile
+};
+
+// One operation as the kernels see it (64-byte aligned, 96 bytes).
+struct alignas(16) Op {
+  double m[8];        // row-major 2x2, (re, im) pairs
+  int32_t target;     // local bit (fused) or qubit (unfused)
+  int32_t ctrl;       // local bit or global qubit, per ctrl_kind
+  int32_t ctrl_kind;  // CtrlKind
+  int32_t cls;        // OpClass
+  int32_t param;      // index of the gradient slot (adjoint) or -1
+  int32_t generator;  // 0 none, 1 X, 2 Y, 3 Z: generator of a rotation (adjoint)
+  int32_t pad[2];
+};
+static_assert(sizeof(Op) == 96, "Op layout");
+
+// Host-side gate after parsing.
+struct Gate {
+  int32_t kind;
+  int32_t target;
+  int32_t control;  // -1 none
+  double theta;
+  double m[8];      // the gate's matrix, computed on the host (gates.cpp)
+  bool observable;
+};
+
+// Matrix of a gate kind, the formulas of the reference's gates.rs.
+void gate_matrix(int32_t kind, double theta, double m[8]);
+int32_t classify(const double m[8]);
+bool is_parametrised(int32_t kind);
+// Generator P of R(theta) = exp(-i theta P / 2): 1 X, 2 Y, 3 Z, 0 none.
+int32_t rotation_generator(int32_t kind);
+// m = a * b (2x2 complex)
+void matmul2(const double a[8], const double b[8], double out[8]);
+// Conjugate transpose.
+void adjoint2(const double a[8], double out[8]);
+int parse_gates(const dmv_gate_t* gates, int64_t num_gates, int32_t n, std::vector<Gate>& out);
+
+// ---------------------------------------------------------------------------
+// Execution plan: a sequence of passes over the statevector.
+// ---------------------------------------------------------------------------
+struct Pass {
+  // kind 0: single op on global qubit indices (unfused kernel).
+  // kind 1: fused window: local bits = [0, low_bits) + high[0..num_high).
+  int32_t kind;
+  int32_t low_bits;
+  int32_t num_high;
+  int32_t high[16];
+  int64_t op_begin;  // range in Plan::ops
+  int64_t op_count;
+};
+
+struct Plan {
+  std::vector<Pass> passes;
+  std::vector<Op> ops;
+  int64_t num_gates = 0;
+};
+
+struct PlanOptions {
+  int32_t fusion = DMV_FUSE_WINDOW;
+  int32_t tile_bits = 12;  // log2 amplitudes per tile
+  int32_t low_bits = 6;    // always-local low qubits (coalesced chunks)
+};
+
+int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
+               const PlanOptions& opt, Plan& plan);
+
+// ---------------------------------------------------------------------------
+// Device state
+// ---------------------------------------------------------------------------
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t n);
+  void release();
+};
+
+}  // namespace dmv
+
+struct dmv_state_s {
+  int32_t n = 0;
+  int64_t N = 0;
+  int32_t precision = DMV_C128;
+  int device = 0;
+  void* amps = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  dmv::DeviceBuffer ops_dev;     // plan ops uploaded for the last apply
+  dmv::DeviceBuffer reduce_dev;  // reduction partials
+  dmv::DeviceBuffer chunk_dev;   // per-chunk probability sums (sampling)
+  std::vector<dmv::Op> ops_host_pinned;  // (regular host memory; copied async from a pinned staging)
+  void* pinned = nullptr;        // pinned host staging
+  size_t pinned_bytes = 0;
+  int64_t last_passes = 0, last_ops = 0, last_bytes = 0;
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  size_t amp_bytes() const { return (size_t)N * (precision == DMV_C128 ? 16 : 8); }
+};
+
+namespace dmv {
+int ensure_pinned(dmv_state_s* s, size_t bytes);
+
+// Kernel launchers (kernels_*.cu). All stream-ordered on s->stream.
+int launch_set_zero(dmv_state_s* s);
+int launch_plan(dmv_state_s* s, const Plan& plan);
+int launch_probabilities(dmv_state_s* s, double* probs_device);
+int launch_expect_z(dmv_state_s* s, double* expect_host, double* norm_host);
+int launch_sample(dmv_state_s* s, const double* uniforms_host, int64_t k, uint64_t* samples_host);
+int sample_from_device_probs(const double* probs_device, int64_t num_probs, int32_t num_bits,
+                             cudaStream_t stream, const double* uniforms_host, int64_t k,
+                             uint64_t* samples_host);
+int launch_inner_product(dmv_state_s* a, dmv_state_s* b, double* re, double* im);
+int launch_scale_by_z_observable(dmv_state_s* dst, dmv_state_s* src, const double* weights_host);
+int launch_adjoint_step(dmv_state_s* psi, dmv_state_s* lam, const Op& op, double* grad_slot_device);
+int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const double* weights,
+                     double* loss, double* grads);
+int upload_ops(dmv_state_s* s, const Op* ops, int64_t count);
+}  // namespace dmv

@@ -1,0 +1,266 @@
+// Gate-application kernels.
+//
+//  * k_apply_single: one 2x2 op over the whole statevector. Each thread owns
+//    whole amplitude pairs (i0, i0 + 2^t), so no amplitude is read after
+//    another thread wrote it (the reference kernel, damavand-gpu/kernels.cu:
+//    120-172, reads every amplitude twice and races across blocks). A
+//    controlled op enumerates only the control=1 quarter-space pairs, so it
+//    moves half the bytes of an uncontrolled one. 64-bit indices throughout.
+//  * k_apply_window: a fused pass. Each CTA stages a tile of 2^k amplitudes
+//    -- the pass's `low` lowest qubits (contiguous 2^low-amplitude chunks in
+//    HBM) times its high local qubits -- in shared memory, applies every op
+//    of the pass to it, and writes it back: one read and one write of the
+//    statevector for the whole window of gates. A control qubit outside the
+//    tile is constant over the tile and is tested once per tile.
+#include <algorithm>
+
+#include "complex_ops.cuh"
+#include "internal.h"
+
+namespace dmv {
+
+namespace {
+
+constexpr int kSingleThreads = 256;
+constexpr int kWindowThreads = 512;
+
+int num_sms() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+template <typename R, int CLS, bool CTRL>
+__global__ void __launch_bounds__(kSingleThreads)
+k_apply_single(typename VecOf<R>::T* __restrict__ a, int64_t num_pairs, int target, int control,
+               M2<R> m) {
+  using V = typename VecOf<R>::T;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int lo = CTRL ? min(target, control) : target;
+  const int hi = CTRL ? max(target, control) : target;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < num_pairs; j += stride) {
+    int64_t i0;
+    if constexpr (CTRL) {
+      i0 = insert_zero(insert_zero(j, lo), hi) | (int64_t(1) << control);
+    } else {
+      i0 = insert_zero(j, target);
+    }
+    const int64_t i1 = i0 | (int64_t(1) << target);
+    V a0 = a[i0];
+    V a1 = a[i1];
+    apply_pair<R, CLS>(m, a0, a1);
+    a[i0] = a0;
+    a[i1] = a1;
+  }
+}
+
+template <typename R, int CLS, bool CTRL>
+void launch_single_t(typename VecOf<R>::T* a, int32_t n, const Op& op, cudaStream_t stream) {
+  const int64_t pairs = (int64_t(1) << n) >> (CTRL ? 2 : 1);
+  const int64_t want = (pairs + kSingleThreads - 1) / kSingleThreads;
+  const int64_t cap = (int64_t)num_sms() * 16;
+  const int grid = (int)std::max<int64_t>(1, std::min(want, cap));
+  k_apply_single<R, CLS, CTRL><<<grid, kSingleThreads, 0, stream>>>(a, pairs, op.target, op.ctrl,
+                                                                     to_m2<R>(op.m));
+}
+
+template <typename R, int CLS>
+void launch_single_c(typename VecOf<R>::T* a, int32_t n, const Op& op, cudaStream_t stream) {
+  if (op.ctrl_kind != CTRL_NONE && op.ctrl >= 0)
+    launch_single_t<R, CLS, true>(a, n, op, stream);
+  else
+    launch_single_t<R, CLS, false>(a, n, op, stream);
+}
+
+template <typename R>
+void launch_single(void* amps, int32_t n, const Op& op, cudaStream_t stream) {
+  using V = typename VecOf<R>::T;
+  V* a = static_cast<V*>(amps);
+  switch (op.cls) {
+    case OP_SWAP: launch_single_c<R, OP_SWAP>(a, n, op, stream); break;
+    case OP_DIAG: launch_single_c<R, OP_DIAG>(a, n, op, stream); break;
+    case OP_ANTI: launch_single_c<R, OP_ANTI>(a, n, op, stream); break;
+    case OP_REAL: launch_single_c<R, OP_REAL>(a, n, op, stream); break;
+    default: launch_single_c<R, OP_GENERAL>(a, n, op, stream); break;
+  }
+}
+
+struct WindowParams {
+  int32_t k;         // log2 tile size
+  int32_t low;       // low local qubits
+  int32_t nh;        // high local qubits
+  int32_t num_ops;
+  int32_t high[16];  // ascending global positions of the high local qubits
+  int64_t num_tiles;
+  const Op* ops;
+};
+
+template <typename R, int CLS, typename V>
+__device__ __forceinline__ void tile_op(V* tile, int T, const Op& op, const M2<R>& m) {
+  const int t = op.target;
+  if (op.ctrl_kind == CTRL_LOCAL) {
+    const int c = op.ctrl;
+    const int lo = min(t, c), hi = max(t, c);
+    for (int q = threadIdx.x; q < (T >> 2); q += blockDim.x) {
+      const uint32_t l0 = insert_zero32(insert_zero32((uint32_t)q, lo), hi) | (1u << c);
+      const uint32_t l1 = l0 | (1u << t);
+      V a0 = tile[l0], a1 = tile[l1];
+      apply_pair<R, CLS>(m, a0, a1);
+      tile[l0] = a0;
+      tile[l1] = a1;
+    }
+  } else {
+    for (int q = threadIdx.x; q < (T >> 1); q += blockDim.x) {
+      const uint32_t l0 = insert_zero32((uint32_t)q, t);
+      const uint32_t l1 = l0 | (1u << t);
+      V a0 = tile[l0], a1 = tile[l1];
+      apply_pair<R, CLS>(m, a0, a1);
+      tile[l0] = a0;
+      tile[l1] = a1;
+    }
+  }
+}
+
+__device__ __forceinline__ int64_t spread_high(uint32_t h, const WindowParams& p) {
+  int64_t off = 0;
+  for (int i = 0; i < p.nh; ++i) off |= (int64_t)((h >> i) & 1u) << p.high[i];
+  return off;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kWindowThreads)
+k_apply_window(typename VecOf<R>::T* __restrict__ a, const WindowParams p) {
+  using V = typename VecOf<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* tile = reinterpret_cast<V*>(smem_raw);
+  const int T = 1 << p.k;
+  const uint32_t lowmask = (1u << p.low) - 1u;
+  for (int64_t tix = blockIdx.x; tix < p.num_tiles; tix += gridDim.x) {
+    int64_t base = tix << p.low;
+    for (int i = 0; i < p.nh; ++i) base = insert_zero(base, p.high[i]);
+    for (int l = threadIdx.x; l < T; l += blockDim.x)
+      tile[l] = a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)];
+    __syncthreads();
+    for (int o = 0; o < p.num_ops; ++o) {
+      const Op& op = p.ops[o];
+      if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1)) continue;  // uniform per tile
+      const M2<R> m = to_m2<R>(op.m);
+      switch (op.cls) {
+        case OP_SWAP: tile_op<R, OP_SWAP>(tile, T, op, m); break;
+        case OP_DIAG: tile_op<R, OP_DIAG>(tile, T, op, m); break;
+        case OP_ANTI: tile_op<R, OP_ANTI>(tile, T, op, m); break;
+        case OP_REAL: tile_op<R, OP_REAL>(tile, T, op, m); break;
+        default: tile_op<R, OP_GENERAL>(tile, T, op, m); break;
+      }
+      __syncthreads();
+    }
+    for (int l = threadIdx.x; l < T; l += blockDim.x)
+      a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)] = tile[l];
+    __syncthreads();
+  }
+}
+
+template <typename R>
+int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cudaStream_t stream) {
+  using V = typename VecOf<R>::T;
+  WindowParams p;
+  p.k = ps.low_bits + ps.num_high;
+  p.low = ps.low_bits;
+  p.nh = ps.num_high;
+  p.num_ops = (int32_t)ps.op_count;
+  for (int i = 0; i < 16; ++i) p.high[i] = i < ps.num_high ? ps.high[i] : 0;
+  p.num_tiles = int64_t(1) << (n - p.k);
+  p.ops = ops_dev + ps.op_begin;
+  const size_t smem = (size_t(1) << p.k) * sizeof(V);
+  static size_t configured = 0;
+  if (smem > configured) {
+    DMV_CUDA_TRY(cudaFuncSetAttribute(k_apply_window<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 48 * 1024)));
+    configured = smem;
+  }
+  int per_sm = 0;
+  DMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_window<R>,
+                                                             kWindowThreads, smem));
+  if (per_sm < 1) return set_error(DMV_ERR_CUDA, "window kernel cannot fit %zu bytes of shared memory", smem);
+  const int64_t grid = std::min<int64_t>(p.num_tiles, (int64_t)per_sm * num_sms());
+  k_apply_window<R><<<(int)grid, kWindowThreads, smem, stream>>>(static_cast<V*>(amps), p);
+  return DMV_OK;
+}
+
+}  // namespace
+
+int upload_ops(dmv_state_s* s, const Op* ops, int64_t count) {
+  if (count <= 0) return DMV_OK;
+  DMV_TRY(s->ops_dev.reserve((size_t)count * sizeof(Op)));
+  DMV_CUDA_TRY(cudaMemcpyAsync(s->ops_dev.ptr, ops, (size_t)count * sizeof(Op),
+                               cudaMemcpyHostToDevice, s->stream));
+  return DMV_OK;
+}
+
+// Multiply-adds one op performs over the whole statevector: GENERAL 16 per
+// amplitude pair, REAL / DIAG / ANTI 8, SWAP none; a control halves it.
+double op_multiply_adds(const Op& op, int64_t N) {
+  double per_pair = 0.;
+  switch (op.cls) {
+    case OP_GENERAL: per_pair = 16.; break;
+    case OP_SWAP: per_pair = 0.; break;
+    default: per_pair = 8.; break;
+  }
+  const double pairs = (double)N / 2.0;
+  return per_pair * pairs * (op.ctrl_kind != CTRL_NONE ? 0.5 : 1.0);
+}
+
+int launch_plan(dmv_state_s* s, const Plan& plan) {
+  bool any_window = false;
+  for (const Pass& ps : plan.passes) any_window |= ps.kind == 1;
+  if (any_window) DMV_TRY(upload_ops(s, plan.ops.data(), (int64_t)plan.ops.size()));
+  const Op* ops_dev = static_cast<const Op*>(s->ops_dev.ptr);
+  int64_t bytes = 0;
+  const int64_t S = (int64_t)s->amp_bytes();
+  for (const Pass& ps : plan.passes) {
+    if (ps.kind == 0) {
+      const Op& op = plan.ops[(size_t)ps.op_begin];
+      const int64_t b = op.ctrl_kind != CTRL_NONE ? S : 2 * S;
+      const int64_t tok = prof_begin(DMV_KERNEL_SINGLE, s->stream, (double)b, op_multiply_adds(op, s->N));
+      if (s->precision == DMV_C128) launch_single<double>(s->amps, s->n, op, s->stream);
+      else launch_single<float>(s->amps, s->n, op, s->stream);
+      prof_end(tok, s->stream);
+      bytes += b;
+    } else {
+      double fmas = 0.;
+      for (int64_t o = 0; o < ps.op_count; ++o) fmas += op_multiply_adds(plan.ops[(size_t)(ps.op_begin + o)], s->N);
+      const int64_t tok = prof_begin(DMV_KERNEL_WINDOW, s->stream, (double)(2 * S), fmas);
+      if (s->precision == DMV_C128) DMV_TRY(launch_window<double>(s->amps, s->n, ps, ops_dev, s->stream));
+      else DMV_TRY(launch_window<float>(s->amps, s->n, ps, ops_dev, s->stream));
+      prof_end(tok, s->stream);
+      bytes += 2 * S;
+    }
+    count_launch();
+  }
+  DMV_CUDA_TRY(cudaGetLastError());
+  s->last_passes = (int64_t)plan.passes.size();
+  s->last_ops = (int64_t)plan.ops.size();
+  s->last_bytes = bytes;
+  return DMV_OK;
+}
+
+// |0...0>: clear the vector and set amplitude 0 to 1 (damavand-gpu/kernels.cu:62-81).
+__global__ void k_set_one(void* amps, int precision) {
+  if (precision == DMV_C128) static_cast<double2*>(amps)[0] = make_double2(1.0, 0.0);
+  else static_cast<float2*>(amps)[0] = make_float2(1.0f, 0.0f);
+}
+
+int launch_set_zero(dmv_state_s* s) {
+  DMV_CUDA_TRY(cudaMemsetAsync(s->amps, 0, s->amp_bytes(), s->stream));
+  k_set_one<<<1, 1, 0, s->stream>>>(s->amps, s->precision);
+  count_launch();
+  DMV_CUDA_TRY(cudaGetLastError());
+  return DMV_OK;
+}
+
+}  // namespace dmv

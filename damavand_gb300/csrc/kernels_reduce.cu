@@ -1,0 +1,624 @@
+// Reductions over the statevector: probabilities, Pauli-Z expectations with
+// per-chunk probability mass, inverse-CDF sampling, inner products, the
+// Z-observable scaling and the adjoint sweep step. All sums accumulate in
+// FP64 (also for complex64 storage) in a fixed order, so results are
+// reproducible run to run.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "complex_ops.cuh"
+#include "internal.h"
+
+namespace dmv {
+
+namespace {
+
+constexpr int kRedThreads = 256;
+constexpr int kMaxChunkBits = 13;  // 8192 amplitudes per chunk
+constexpr int kRowsPerThread = 32; // (1 << kMaxChunkBits) / kRedThreads
+
+int sm_count() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum (all threads get the result). `red` has >= 32 doubles.
+__device__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.;
+  const int nw = (blockDim.x + 31) >> 5;
+  if (warp == 0) {
+    t = lane < nw ? red[lane] : 0.;
+    t = warp_sum(t);
+    if (lane == 0) red[0] = t;
+  }
+  __syncthreads();
+  t = red[0];
+  __syncthreads();
+  return t;
+}
+
+// Probability of element i from one of three sources.
+template <int SRC>
+__device__ __forceinline__ double prob_at(const void* src, int64_t i) {
+  if constexpr (SRC == 0) return norm2(static_cast<const double2*>(src)[i]);
+  else if constexpr (SRC == 1) return norm2(static_cast<const float2*>(src)[i]);
+  else return static_cast<const double*>(src)[i];
+}
+
+template <int SRC>
+__global__ void __launch_bounds__(kRedThreads)
+k_probabilities(const void* src, double* __restrict__ out, int64_t N) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride)
+    out[i] = prob_at<SRC>(src, i);
+}
+
+// Per-chunk probability mass and per-qubit "bit set" mass.
+// Element e of a chunk is e = tid + 256*r. Each thread keeps one accumulator
+// per r across all chunks it visits, so the inner loop costs one FP64 add per
+// element; the bit sums are formed once per CTA at the end.
+// partial[cta * (n+1) + q] = sum of p over indices with bit q set, q < n;
+// partial[cta * (n+1) + n] = sum of all p.
+template <int SRC>
+__global__ void __launch_bounds__(kRedThreads)
+k_chunk_mass(const void* src, int n, int chunk_bits, int64_t num_chunks,
+             double* __restrict__ chunk_mass, double* __restrict__ partial) {
+  __shared__ double red[32];
+  __shared__ double tsum[kRedThreads];
+  __shared__ double rsum[5][kRedThreads];
+  const int C = 1 << chunk_bits;
+  double v[kRowsPerThread];
+#pragma unroll
+  for (int r = 0; r < kRowsPerThread; ++r) v[r] = 0.;
+  __shared__ double hi_acc[34];  // only thread 0 updates it
+  if (threadIdx.x < 34) hi_acc[threadIdx.x] = 0.;
+
+  for (int64_t ch = blockIdx.x; ch < num_chunks; ch += gridDim.x) {
+    const int64_t base = ch << chunk_bits;
+    double mine = 0.;
+#pragma unroll
+    for (int r = 0; r < kRowsPerThread; ++r) {
+      const int e = threadIdx.x + kRedThreads * r;
+      if (e < C) {
+        const double p = prob_at<SRC>(src, base + e);
+        v[r] += p;
+        mine += p;
+      }
+    }
+    const double tot = block_sum(mine, red);
+    if (threadIdx.x == 0) {
+      chunk_mass[ch] = tot;
+      for (int j = 0; j < n - chunk_bits; ++j)
+        if ((ch >> j) & 1) hi_acc[j] += tot;
+    }
+  }
+  // Fold per-thread accumulators into bit sums.
+  double T = 0.;
+  double R[5] = {0., 0., 0., 0., 0.};
+#pragma unroll
+  for (int r = 0; r < kRowsPerThread; ++r) {
+    T += v[r];
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+      if ((r >> j) & 1) R[j] += v[r];
+  }
+  tsum[threadIdx.x] = T;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) rsum[j][threadIdx.x] = R[j];
+  __syncthreads();
+  double* out = partial + (int64_t)blockIdx.x * (n + 1);
+  const int q = threadIdx.x;
+  if (q < chunk_bits) {
+    double acc = 0.;
+    if (q < 8) {
+      for (int t = 0; t < kRedThreads; ++t)
+        if ((t >> q) & 1) acc += tsum[t];
+    } else {
+      for (int t = 0; t < kRedThreads; ++t) acc += rsum[q - 8][t];
+    }
+    out[q] = acc;
+  } else if (q == 64) {
+    double acc = 0.;
+    for (int t = 0; t < kRedThreads; ++t) acc += tsum[t];
+    out[n] = acc;
+  }
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < n - chunk_bits; ++j) out[chunk_bits + j] = hi_acc[j];
+  }
+}
+
+// Sum the per-CTA partials in CTA order.
+__global__ void k_reduce_partials(const double* __restrict__ partial, int width, int rows,
+                                  double* __restrict__ out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= width) return;
+  double acc = 0.;
+  for (int r = 0; r < rows; ++r) acc += partial[(int64_t)r * width + q];
+  out[q] = acc;
+}
+
+// out[r] = sum_c in[r * cols + c], in column order.
+__global__ void k_reduce_rows(const double* __restrict__ in, int64_t rows, int cols, double* __restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  double acc = 0.;
+  for (int c = 0; c < cols; ++c) acc += in[r * cols + c];
+  out[r] = acc;
+}
+
+// Inclusive prefix of the chunk masses (one CTA, fixed order).
+__global__ void __launch_bounds__(1024)
+k_scan_chunks(const double* __restrict__ mass, int64_t num_chunks, double* __restrict__ incl) {
+  __shared__ double seg[1024];
+  const int64_t per = (num_chunks + blockDim.x - 1) / blockDim.x;
+  const int64_t b = (int64_t)threadIdx.x * per;
+  const int64_t e = min(num_chunks, b + per);
+  double s = 0.;
+  for (int64_t i = b; i < e; ++i) s += mass[i];
+  seg[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {  // 1024 serial adds: negligible next to the pass over HBM
+    double run = 0.;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      const double x = seg[t];
+      seg[t] = run;
+      run += x;
+    }
+  }
+  __syncthreads();
+  double run = seg[threadIdx.x];
+  for (int64_t i = b; i < e; ++i) {
+    run += mass[i];
+    incl[i] = run;
+  }
+}
+
+// One CTA per sample. Finds the least index with u*total <= cdf(index), the
+// rule of src/utils.rs:258-277 (cdf(index) = p_0 + ... + p_index).
+template <int SRC>
+__global__ void __launch_bounds__(kRedThreads)
+k_sample(const void* src, int chunk_bits, int64_t num_chunks, const double* __restrict__ incl,
+         const double* __restrict__ uniforms, int64_t k, uint64_t* __restrict__ samples) {
+  __shared__ double scan[kRedThreads];
+  __shared__ long long best;
+  __shared__ long long last_nonzero;
+  const int C = 1 << chunk_bits;
+  const double total = incl[num_chunks - 1];
+  for (int64_t s = blockIdx.x; s < k; s += gridDim.x) {
+    const double xsi = uniforms[s] * total;
+    if (!(xsi > 0.)) {  // xsi == 0 matches cdf[0] = 0: the reference returns 0 - 1
+      if (threadIdx.x == 0) samples[s] = ~uint64_t(0);
+      continue;
+    }
+    // least chunk whose inclusive mass reaches xsi
+    int64_t lo = 0, hi = num_chunks - 1;
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo) / 2;
+      if (xsi <= incl[mid]) hi = mid; else lo = mid + 1;
+    }
+    const int64_t ch = lo;
+    const double before = ch > 0 ? incl[ch - 1] : 0.;
+    const int per = (C + kRedThreads - 1) / kRedThreads;
+    const int64_t base = (ch << chunk_bits);
+    const int e0 = threadIdx.x * per;
+    double mine = 0.;
+    for (int j = 0; j < per; ++j)
+      if (e0 + j < C) mine += prob_at<SRC>(src, base + e0 + j);
+    scan[threadIdx.x] = mine;
+    if (threadIdx.x == 0) { best = LLONG_MAX; last_nonzero = -1; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double run = 0.;
+      for (int t = 0; t < kRedThreads; ++t) { const double x = scan[t]; scan[t] = run; run += x; }
+    }
+    __syncthreads();
+    double run = before + scan[threadIdx.x];
+    long long found = LLONG_MAX, nz = -1;
+    for (int j = 0; j < per; ++j) {
+      const int e = e0 + j;
+      if (e >= C) break;
+      const double p = prob_at<SRC>(src, base + e);
+      run += p;
+      if (p > 0.) nz = base + e;
+      if (xsi <= run) { found = base + e; break; }
+    }
+    if (found != LLONG_MAX) atomicMin(&best, found);
+    if (nz >= 0) atomicMax(&last_nonzero, nz);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long r = best;
+      if (r == LLONG_MAX) r = last_nonzero >= 0 ? last_nonzero : (long long)(base + C - 1);
+      samples[s] = (uint64_t)r;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kRedThreads)
+k_inner(const V* __restrict__ a, const V* __restrict__ b, int64_t N, double* __restrict__ partial) {
+  __shared__ double red[32];
+  double re = 0., im = 0.;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    const double ar = a[i].x, ai = a[i].y, br = b[i].x, bi = b[i].y;
+    re = fma(ar, br, fma(ai, bi, re));
+    im = fma(ar, bi, fma(-ai, br, im));
+  }
+  re = block_sum(re, red);
+  im = block_sum(im, red);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = re;
+    partial[2 * blockIdx.x + 1] = im;
+  }
+}
+
+// dst_i = d(i) * src_i with d(i) = sum_q w_q (1 - 2 bit_q(i)), from four
+// 1024-entry tables over 10-bit index fields.
+template <typename V>
+__global__ void __launch_bounds__(kRedThreads)
+k_scale_z(V* __restrict__ dst, const V* __restrict__ src, int64_t N, const double* __restrict__ tables) {
+  __shared__ double tab[4 * 1024];
+  for (int i = threadIdx.x; i < 4 * 1024; i += blockDim.x) tab[i] = tables[i];
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    const double d = tab[i & 1023] + tab[1024 + ((i >> 10) & 1023)] + tab[2048 + ((i >> 20) & 1023)] +
+                     tab[3072 + ((i >> 30) & 1023)];
+    V v = src[i];
+    v.x = (decltype(v.x))((double)v.x * d);
+    v.y = (decltype(v.y))((double)v.y * d);
+    dst[i] = v;
+  }
+}
+
+// One step of the adjoint sweep for gate U (op holds U^dagger):
+//   grad += Im <lam| P |psi>   (P the rotation's generator, pre-update values)
+//   psi <- U^dagger psi, lam <- U^dagger lam.
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads)
+k_adjoint_step(typename VecOf<R>::T* __restrict__ psi, typename VecOf<R>::T* __restrict__ lam,
+               int64_t num_pairs, Op op, int apply, double* __restrict__ partial) {
+  using V = typename VecOf<R>::T;
+  __shared__ double red[32];
+  const M2<R> m = to_m2<R>(op.m);
+  const int t = op.target;
+  const bool ctrl = op.ctrl_kind != CTRL_NONE && op.ctrl >= 0;
+  const int c = op.ctrl;
+  const int lo = ctrl ? min(t, c) : t, hi = ctrl ? max(t, c) : t;
+  const int gen = op.generator;
+  double acc = 0.;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < num_pairs; j += stride) {
+    int64_t i0 = ctrl ? (insert_zero(insert_zero(j, lo), hi) | (int64_t(1) << c)) : insert_zero(j, t);
+    const int64_t i1 = i0 | (int64_t(1) << t);
+    V p0 = psi[i0], p1 = psi[i1], l0 = lam[i0], l1 = lam[i1];
+    if (gen != 0) {
+      const double p0r = p0.x, p0i = p0.y, p1r = p1.x, p1i = p1.y;
+      const double l0r = l0.x, l0i = l0.y, l1r = l1.x, l1i = l1.y;
+      if (gen == 1) {        // X: Im(l0* p1) + Im(l1* p0)
+        acc += fma(l0r, p1i, -l0i * p1r) + fma(l1r, p0i, -l1i * p0r);
+      } else if (gen == 2) { // Y: -Re(l0* p1) + Re(l1* p0)
+        acc += -fma(l0r, p1r, l0i * p1i) + fma(l1r, p0r, l1i * p0i);
+      } else {               // Z: Im(l0* p0) - Im(l1* p1)
+        acc += fma(l0r, p0i, -l0i * p0r) - fma(l1r, p1i, -l1i * p1r);
+      }
+    }
+    if (apply) {
+      apply_pair_dyn<R>(op.cls, m, p0, p1);
+      apply_pair_dyn<R>(op.cls, m, l0, l1);
+      psi[i0] = p0; psi[i1] = p1;
+      lam[i0] = l0; lam[i1] = l1;
+    }
+  }
+  if (gen != 0) {
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+  }
+}
+
+int chunk_bits_for(int n) { return std::min(kMaxChunkBits, n); }
+
+int grid_for_chunks(int64_t num_chunks) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(num_chunks, (int64_t)sm_count() * 8));
+}
+
+// Runs k_chunk_mass and the partial reduction. Leaves chunk masses in
+// chunk_dev and the n+1 sums (bit-set mass per qubit, then total) in `sums_dev`.
+int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& chunk_dev,
+                    DeviceBuffer& reduce_dev, cudaStream_t stream, double** sums_dev_out,
+                    int64_t* num_chunks_out, int* chunk_bits_out) {
+  const int cb = chunk_bits_for(n);
+  const int64_t num_chunks = int64_t(1) << (n - cb);
+  const int grid = grid_for_chunks(num_chunks);
+  DMV_TRY(chunk_dev.reserve((size_t)num_chunks * sizeof(double)));
+  const size_t partial_elems = (size_t)grid * (n + 1);
+  DMV_TRY(reduce_dev.reserve((partial_elems + (size_t)(n + 1)) * sizeof(double)));
+  double* partial = static_cast<double*>(reduce_dev.ptr);
+  double* sums = partial + partial_elems;
+  double* mass = static_cast<double*>(chunk_dev.ptr);
+  switch (src_kind) {
+    case 0: k_chunk_mass<0><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
+    case 1: k_chunk_mass<1><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
+    default: k_chunk_mass<2><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
+  }
+  k_reduce_partials<<<1, 64, 0, stream>>>(partial, n + 1, grid, sums);
+  count_launch(2);
+  DMV_CUDA_TRY(cudaGetLastError());
+  *sums_dev_out = sums;
+  *num_chunks_out = num_chunks;
+  *chunk_bits_out = cb;
+  return DMV_OK;
+}
+
+int run_sampler(const void* src, int src_kind, int chunk_bits, int64_t num_chunks,
+                const double* mass, DeviceBuffer& scratch, cudaStream_t stream,
+                const double* uniforms_host, int64_t k, uint64_t* samples_host) {
+  if (k <= 0) return DMV_OK;
+  const size_t need = (size_t)num_chunks * sizeof(double) + (size_t)k * (sizeof(double) + sizeof(uint64_t));
+  DMV_TRY(scratch.reserve(need));
+  double* incl = static_cast<double*>(scratch.ptr);
+  double* u_dev = incl + num_chunks;
+  uint64_t* out_dev = reinterpret_cast<uint64_t*>(u_dev + k);
+  DMV_CUDA_TRY(cudaMemcpyAsync(u_dev, uniforms_host, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, stream));
+  k_scan_chunks<<<1, 1024, 0, stream>>>(mass, num_chunks, incl);
+  const int grid = (int)std::min<int64_t>(k, (int64_t)sm_count() * 8);
+  switch (src_kind) {
+    case 0: k_sample<0><<<grid, kRedThreads, 0, stream>>>(src, chunk_bits, num_chunks, incl, u_dev, k, out_dev); break;
+    case 1: k_sample<1><<<grid, kRedThreads, 0, stream>>>(src, chunk_bits, num_chunks, incl, u_dev, k, out_dev); break;
+    default: k_sample<2><<<grid, kRedThreads, 0, stream>>>(src, chunk_bits, num_chunks, incl, u_dev, k, out_dev); break;
+  }
+  count_launch(2);
+  DMV_CUDA_TRY(cudaGetLastError());
+  DMV_CUDA_TRY(cudaMemcpyAsync(samples_host, out_dev, (size_t)k * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+  DMV_CUDA_TRY(cudaStreamSynchronize(stream));
+  return DMV_OK;
+}
+
+}  // namespace
+
+int launch_probabilities(dmv_state_s* s, double* probs_device) {
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((s->N + kRedThreads - 1) / kRedThreads,
+                                                               (int64_t)sm_count() * 16));
+  if (s->precision == DMV_C128)
+    k_probabilities<0><<<grid, kRedThreads, 0, s->stream>>>(s->amps, probs_device, s->N);
+  else
+    k_probabilities<1><<<grid, kRedThreads, 0, s->stream>>>(s->amps, probs_device, s->N);
+  count_launch();
+  DMV_CUDA_TRY(cudaGetLastError());
+  return DMV_OK;
+}
+
+int launch_expect_z(dmv_state_s* s, double* expect_host, double* norm_host) {
+  double* sums = nullptr;
+  int64_t nc = 0;
+  int cb = 0;
+  DMV_TRY(chunk_mass_pass(s->amps, s->precision == DMV_C128 ? 0 : 1, s->n, s->chunk_dev, s->reduce_dev,
+                          s->stream, &sums, &nc, &cb));
+  std::vector<double> h((size_t)s->n + 1);
+  DMV_CUDA_TRY(cudaMemcpyAsync(h.data(), sums, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  const double total = h[(size_t)s->n];
+  if (expect_host)
+    for (int q = 0; q < s->n; ++q) expect_host[q] = total - 2.0 * h[(size_t)q];
+  if (norm_host) *norm_host = total;
+  return DMV_OK;
+}
+
+int launch_sample(dmv_state_s* s, const double* uniforms_host, int64_t k, uint64_t* samples_host) {
+  double* sums = nullptr;
+  int64_t nc = 0;
+  int cb = 0;
+  const int src_kind = s->precision == DMV_C128 ? 0 : 1;
+  DMV_TRY(chunk_mass_pass(s->amps, src_kind, s->n, s->chunk_dev, s->reduce_dev, s->stream, &sums, &nc, &cb));
+  return run_sampler(s->amps, src_kind, cb, nc, static_cast<const double*>(s->chunk_dev.ptr), s->reduce_dev,
+                     s->stream, uniforms_host, k, samples_host);
+}
+
+int sample_from_device_probs(const double* probs_device, int64_t num_probs, int32_t num_bits,
+                             cudaStream_t stream, const double* uniforms_host, int64_t k,
+                             uint64_t* samples_host) {
+  (void)num_probs;
+  DeviceBuffer chunk_dev, reduce_dev, scratch;
+  double* sums = nullptr;
+  int64_t nc = 0;
+  int cb = 0;
+  int rc = chunk_mass_pass(probs_device, 2, num_bits, chunk_dev, reduce_dev, stream, &sums, &nc, &cb);
+  if (rc == DMV_OK)
+    rc = run_sampler(probs_device, 2, cb, nc, static_cast<const double*>(chunk_dev.ptr), scratch, stream,
+                     uniforms_host, k, samples_host);
+  cudaStreamSynchronize(stream);
+  chunk_dev.release();
+  reduce_dev.release();
+  scratch.release();
+  return rc;
+}
+
+int launch_inner_product(dmv_state_s* a, dmv_state_s* b, double* re, double* im) {
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((a->N + kRedThreads - 1) / kRedThreads,
+                                                               (int64_t)sm_count() * 8));
+  DMV_TRY(a->reduce_dev.reserve((size_t)(2 * grid + 2) * sizeof(double)));
+  double* partial = static_cast<double*>(a->reduce_dev.ptr);
+  double* sums = partial + 2 * grid;
+  // b's pending work must be complete before a's stream reads it.
+  if (a->stream != b->stream) {
+    cudaEvent_t ev;
+    DMV_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, b->stream);
+    cudaStreamWaitEvent(a->stream, ev, 0);
+    cudaEventDestroy(ev);
+  }
+  if (a->precision == DMV_C128)
+    k_inner<double2><<<grid, kRedThreads, 0, a->stream>>>(static_cast<const double2*>(a->amps),
+                                                         static_cast<const double2*>(b->amps), a->N, partial);
+  else
+    k_inner<float2><<<grid, kRedThreads, 0, a->stream>>>(static_cast<const float2*>(a->amps),
+                                                        static_cast<const float2*>(b->amps), a->N, partial);
+  k_reduce_partials<<<1, 64, 0, a->stream>>>(partial, 2, grid, sums);
+  count_launch(2);
+  DMV_CUDA_TRY(cudaGetLastError());
+  double h[2];
+  DMV_CUDA_TRY(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, a->stream));
+  DMV_CUDA_TRY(cudaStreamSynchronize(a->stream));
+  *re = h[0];
+  *im = h[1];
+  return DMV_OK;
+}
+
+int launch_scale_by_z_observable(dmv_state_s* dst, dmv_state_s* src, const double* weights_host) {
+  std::vector<double> tab(4 * 1024, 0.0);
+  for (int f = 0; f < 4; ++f)
+    for (int x = 0; x < 1024; ++x) {
+      double acc = 0.;
+      for (int b = 0; b < 10; ++b) {
+        const int q = 10 * f + b;
+        if (q >= src->n) break;
+        acc += ((x >> b) & 1) ? -weights_host[q] : weights_host[q];
+      }
+      tab[(size_t)f * 1024 + (size_t)x] = acc;
+    }
+  DMV_TRY(dst->reduce_dev.reserve(tab.size() * sizeof(double)));
+  DMV_CUDA_TRY(cudaMemcpyAsync(dst->reduce_dev.ptr, tab.data(), tab.size() * sizeof(double),
+                               cudaMemcpyHostToDevice, dst->stream));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((src->N + kRedThreads - 1) / kRedThreads,
+                                                               (int64_t)sm_count() * 8));
+  if (src->precision == DMV_C128)
+    k_scale_z<double2><<<grid, kRedThreads, 0, dst->stream>>>(
+        static_cast<double2*>(dst->amps), static_cast<const double2*>(src->amps), src->N,
+        static_cast<const double*>(dst->reduce_dev.ptr));
+  else
+    k_scale_z<float2><<<grid, kRedThreads, 0, dst->stream>>>(
+        static_cast<float2*>(dst->amps), static_cast<const float2*>(src->amps), src->N,
+        static_cast<const double*>(dst->reduce_dev.ptr));
+  count_launch();
+  DMV_CUDA_TRY(cudaGetLastError());
+  // The table buffer is reused by the next call on this stream only after
+  // this kernel, by stream order.
+  return DMV_OK;
+}
+
+int adjoint_grid(int64_t num_pairs) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((num_pairs + kRedThreads - 1) / kRedThreads,
+                                                      (int64_t)sm_count() * 8));
+}
+
+int launch_adjoint_step_impl(dmv_state_s* psi, dmv_state_s* lam, const Op& op, int apply,
+                             double* partial_slot) {
+  const bool ctrl = op.ctrl_kind != CTRL_NONE && op.ctrl >= 0;
+  const int64_t pairs = psi->N >> (ctrl ? 2 : 1);
+  const int grid = adjoint_grid(pairs);
+  if (psi->precision == DMV_C128)
+    k_adjoint_step<double><<<grid, kRedThreads, 0, psi->stream>>>(
+        static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
+  else
+    k_adjoint_step<float><<<grid, kRedThreads, 0, psi->stream>>>(
+        static_cast<float2*>(psi->amps), static_cast<float2*>(lam->amps), pairs, op, apply, partial_slot);
+  count_launch();
+  DMV_CUDA_TRY(cudaGetLastError());
+  return DMV_OK;
+}
+
+int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const double* weights,
+                     double* loss, double* grads) {
+  // Forward from |0...0> with the fused plan.
+  DMV_TRY(launch_set_zero(s));
+  Plan plan;
+  PlanOptions opt;
+  DMV_TRY(build_plan(gates, s->n, s->precision, opt, plan));
+  DMV_TRY(launch_plan(s, plan));
+  std::vector<double> ez((size_t)s->n);
+  DMV_TRY(launch_expect_z(s, ez.data(), nullptr));
+  double L = 0.;
+  for (int q = 0; q < s->n; ++q) L += weights[q] * ez[(size_t)q];
+  if (loss) *loss = L;
+
+  // Parameter slots in list order (Circuit::set_parameters order).
+  std::vector<int64_t> slot_of(gates.size(), -1);
+  int64_t num_params = 0;
+  for (size_t i = 0; i < gates.size(); ++i)
+    if (!gates[i].observable && is_parametrised(gates[i].kind)) slot_of[i] = num_params++;
+  if (num_params == 0) return DMV_OK;
+
+  dmv_state_t psi = nullptr, lam = nullptr;
+  int rc = dmv_state_create(s->n, s->precision, s->stream, &psi);
+  if (rc != DMV_OK) return rc;
+  rc = dmv_state_create(s->n, s->precision, s->stream, &lam);
+  if (rc != DMV_OK) { dmv_state_destroy(psi); return rc; }
+
+  DeviceBuffer partial;
+  const int64_t pairs_u = s->N >> 1;
+  const int grid = adjoint_grid(pairs_u);
+  do {
+    rc = partial.reserve((size_t)num_params * grid * sizeof(double) + (size_t)num_params * sizeof(double));
+    if (rc != DMV_OK) break;
+    double* part = static_cast<double*>(partial.ptr);
+    double* out = part + (size_t)num_params * grid;
+    if (cudaMemsetAsync(part, 0, (size_t)num_params * grid * sizeof(double), s->stream) != cudaSuccess) {
+      rc = set_error(DMV_ERR_CUDA, "memset of gradient partials failed");
+      break;
+    }
+    if (cudaMemcpyAsync(psi->amps, s->amps, s->amp_bytes(), cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess) {
+      rc = set_error(DMV_ERR_CUDA, "statevector copy failed");
+      break;
+    }
+    rc = launch_scale_by_z_observable(lam, s, weights);
+    if (rc != DMV_OK) break;
+    for (int64_t gi = (int64_t)gates.size() - 1; gi >= 0 && rc == DMV_OK; --gi) {
+      const Gate& g = gates[(size_t)gi];
+      if (g.observable) continue;
+      Op op;
+      std::memset(&op, 0, sizeof(op));
+      adjoint2(g.m, op.m);
+      op.target = g.target;
+      op.ctrl = g.control;
+      op.ctrl_kind = g.control >= 0 ? CTRL_GLOBAL : CTRL_NONE;
+      op.cls = classify(op.m);
+      op.param = (int32_t)slot_of[(size_t)gi];
+      op.generator = slot_of[(size_t)gi] >= 0 ? rotation_generator(g.kind) : 0;
+      // The grid of k_adjoint_step depends on the pair count; partials of
+      // controlled parametrised gates use fewer CTAs and leave zeros behind.
+      double* slot = op.param >= 0 ? part + (size_t)op.param * grid : part;
+      const bool last = gi == 0;
+      rc = launch_adjoint_step_impl(psi, lam, op, last ? 0 : 1, slot);
+    }
+    if (rc != DMV_OK) break;
+    k_reduce_rows<<<(int)((num_params + 127) / 128), 128, 0, s->stream>>>(part, num_params, grid, out);
+    count_launch();
+    if (cudaMemcpyAsync(grads, out, (size_t)num_params * sizeof(double), cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+        cudaStreamSynchronize(s->stream) != cudaSuccess) {
+      rc = set_error(DMV_ERR_CUDA, "gradient readback failed");
+      break;
+    }
+  } while (false);
+  cudaStreamSynchronize(s->stream);
+  partial.release();
+  dmv_state_destroy(psi);
+  dmv_state_destroy(lam);
+  return rc;
+}
+
+int launch_adjoint_step(dmv_state_s* psi, dmv_state_s* lam, const Op& op, double* grad_slot_device) {
+  return launch_adjoint_step_impl(psi, lam, op, 1, grad_slot_device);
+}
+
+}  // namespace dmv

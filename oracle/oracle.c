@@ -1,0 +1,241 @@
+/*
+ * CPU oracle (test infrastructure only) -- see oracle.h for scope and pinning.
+ * Each function cites the reference lines it restates.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* num-complex Mul: (a.re*b.re - a.im*b.im, a.re*b.im + a.im*b.re), no FMA. */
+static inline void cmul(double ar, double ai, double br, double bi, double* cr, double* ci) {
+  *cr = ar * br - ai * bi;
+  *ci = ar * bi + ai * br;
+}
+
+/* Matrices of src/qubit_backend/gates.rs: Hadamard :97-119, PauliX :223-233,
+ * PauliY :288-298, PauliZ :352-362, RotationX :417-439, RotationY :489-511,
+ * RotationZ :561-577; CNOT uses the PauliX matrix (circuit_multithreading.rs:14-20). */
+void orc_gate_matrix(int32_t kind, double theta, double m[8]) {
+  memset(m, 0, 8 * sizeof(double));
+  switch (kind) {
+    case ORC_H: {
+      double h = 1. / sqrt(2.0);
+      m[0] = h; m[2] = h; m[4] = h; m[6] = -1. / sqrt(2.0);
+      break;
+    }
+    case ORC_X:
+    case ORC_CNOT:
+      m[2] = 1.; m[4] = 1.;
+      break;
+    case ORC_Y:
+      m[3] = -1.; m[5] = 1.;
+      break;
+    case ORC_Z:
+      m[0] = 1.; m[6] = -1.;
+      break;
+    case ORC_RX:
+      m[0] = cos(theta / 2.); m[3] = -sin(theta / 2.);
+      m[5] = -sin(theta / 2.); m[6] = cos(theta / 2.);
+      break;
+    case ORC_RY:
+      m[0] = cos(theta / 2.); m[2] = -sin(theta / 2.);
+      m[4] = sin(theta / 2.); m[6] = cos(theta / 2.);
+      break;
+    case ORC_RZ:
+      m[0] = cos(-theta / 2.); m[1] = sin(-theta / 2.);
+      m[6] = cos(theta / 2.); m[7] = sin(theta / 2.);
+      break;
+    default:
+      break;
+  }
+}
+
+/* Circuit::new / reset_amplitudes for the CPU paths: zeros, amplitude 0 = 1
+ * (src/qubit_backend/circuit.rs:172-175, :262-267). */
+void orc_zero_state(double* state, int32_t n) {
+  int64_t N = (int64_t)1 << n;
+  memset(state, 0, (size_t)N * 2 * sizeof(double));
+  state[0] = 1.;
+}
+
+/* Circuit::compute_partner_rank(i, 1, gap), src/qubit_backend/circuit.rs:781-795. */
+static inline int64_t partner_index(int64_t i, int64_t gap) {
+  return (i % (2 * gap)) < gap ? i + gap : i - gap;
+}
+
+/* apply_multithreading_local, src/qubit_backend/circuit_multithreading.rs:9-54. */
+void orc_apply_gate(double* state, double* scratch, int32_t n, const double m[8],
+                    int32_t control, int32_t target) {
+  int64_t N = (int64_t)1 << n;
+  int64_t gap = (int64_t)1 << target;
+  memcpy(scratch, state, (size_t)N * 2 * sizeof(double)); /* :31 clone */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) {
+    int apply = control < 0 ? 1 : (int)((i >> control) & 1); /* :35-39 */
+    if (!apply) continue;
+    int64_t p = partner_index(i, gap); /* :40-41 */
+    double ar = state[2 * i], ai = state[2 * i + 1];
+    double pr = scratch[2 * p], pi = scratch[2 * p + 1];
+    double t0r, t0i, t1r, t1i;
+    if (p > i) { /* :46-47  a*m00 + partner*m01 */
+      cmul(ar, ai, m[0], m[1], &t0r, &t0i);
+      cmul(pr, pi, m[2], m[3], &t1r, &t1i);
+    } else {     /* :48-49  partner*m10 + a*m11 */
+      cmul(pr, pi, m[4], m[5], &t0r, &t0i);
+      cmul(ar, ai, m[6], m[7], &t1r, &t1i);
+    }
+    state[2 * i] = t0r + t1r;
+    state[2 * i + 1] = t0i + t1i;
+  }
+}
+
+/* Circuit::forward, src/qubit_backend/circuit.rs:341-369: observables skipped. */
+void orc_forward(double* state, int32_t n, const orc_gate* gates, int64_t num_gates) {
+  int64_t N = (int64_t)1 << n;
+  double* scratch = (double*)malloc((size_t)N * 2 * sizeof(double));
+  if (!scratch) return;
+  for (int64_t g = 0; g < num_gates; ++g) {
+    if (gates[g].is_observable) continue;
+    double m[8];
+    orc_gate_matrix(gates[g].kind, gates[g].theta, m);
+    int32_t control = gates[g].kind == ORC_CNOT ? gates[g].control : -1;
+    orc_apply_gate(state, scratch, n, m, control, gates[g].target);
+  }
+  free(scratch);
+}
+
+/* Circuit::measure CPU branch, src/qubit_backend/circuit.rs:579-581 (norm_sqr). */
+void orc_measure(const double* state, int32_t n, double* probs) {
+  int64_t N = (int64_t)1 << n;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i)
+    probs[i] = state[2 * i] * state[2 * i] + state[2 * i + 1] * state[2 * i + 1];
+}
+
+/* utils::sample_from_discrete_distribution + sample_from_discrete_cumulative,
+ * src/utils.rs:258-277, with the thread_rng draw replaced by `u`. */
+uint64_t orc_sample_one(const double* probs, int64_t num_probs, double u) {
+  /* cumulative = [0, p0, p0+p1, ...] built sequentially (:270-274) */
+  double* cdf = (double*)malloc((size_t)(num_probs + 1) * sizeof(double));
+  if (!cdf) return UINT64_MAX;
+  cdf[0] = 0.;
+  for (int64_t j = 0; j < num_probs; ++j) cdf[j + 1] = cdf[j] + probs[j];
+  double xsi = u * cdf[num_probs]; /* :260 */
+  uint64_t result = UINT64_MAX;    /* None -> the caller panics (circuit.rs:478-482) */
+  for (int64_t idx = 0; idx <= num_probs; ++idx) { /* :262-266 */
+    if (xsi <= cdf[idx]) { result = (uint64_t)idx - 1u; break; }
+  }
+  free(cdf);
+  return result;
+}
+
+void orc_sample(const double* probs, int64_t num_probs, const double* uniforms,
+                int64_t k, uint64_t* samples, int32_t rebuild_per_sample) {
+  if (rebuild_per_sample) { /* Circuit::sample_local, circuit.rs:468-485 */
+    for (int64_t s = 0; s < k; ++s) samples[s] = orc_sample_one(probs, num_probs, uniforms[s]);
+    return;
+  }
+  double* cdf = (double*)malloc((size_t)(num_probs + 1) * sizeof(double));
+  if (!cdf) return;
+  cdf[0] = 0.;
+  for (int64_t j = 0; j < num_probs; ++j) cdf[j + 1] = cdf[j] + probs[j];
+#pragma omp parallel for schedule(static)
+  for (int64_t s = 0; s < k; ++s) {
+    double xsi = uniforms[s] * cdf[num_probs];
+    int64_t lo = 0, hi = num_probs + 1; /* least idx in [0, N] with xsi <= cdf[idx] */
+    while (lo < hi) {
+      int64_t mid = lo + (hi - lo) / 2;
+      if (xsi <= cdf[mid]) hi = mid; else lo = mid + 1;
+    }
+    samples[s] = lo <= num_probs ? (uint64_t)lo - 1u : UINT64_MAX;
+  }
+  free(cdf);
+}
+
+/* Exact Pauli-Z expectation; sign convention of circuit.rs:503-508 (+1 for bit 0). */
+void orc_expect_z(const double* probs, int32_t n, double* out) {
+  int64_t N = (int64_t)1 << n;
+  for (int32_t q = 0; q < n; ++q) {
+    double acc = 0.;
+#pragma omp parallel for schedule(static) reduction(+ : acc)
+    for (int64_t i = 0; i < N; ++i) acc += ((i >> q) & 1) ? -probs[i] : probs[i];
+    out[q] = acc;
+  }
+}
+
+/* Circuit::extract_expectation_values, src/qubit_backend/circuit.rs:494-513. */
+void orc_extract_expectation_values(const uint64_t* samples, int64_t k,
+                                    const int32_t* readout_qubits, int32_t num_obs,
+                                    double* out) {
+  for (int64_t s = 0; s < k; ++s)
+    for (int32_t j = 0; j < num_obs; ++j)
+      out[s * num_obs + j] = ((samples[s] >> (readout_qubits[j] & 63)) & 1) ? -1. : 1.;
+}
+
+static int is_parametrised(int32_t kind) {
+  return kind == ORC_RX || kind == ORC_RY || kind == ORC_RZ;
+}
+
+double orc_loss(int32_t n, const orc_gate* gates, int64_t num_gates,
+                const double* params, int64_t num_params, const double* weights) {
+  int64_t N = (int64_t)1 << n;
+  orc_gate* g = (orc_gate*)malloc((size_t)num_gates * sizeof(orc_gate));
+  double* state = (double*)malloc((size_t)N * 2 * sizeof(double));
+  double* probs = (double*)malloc((size_t)N * sizeof(double));
+  double* ez = (double*)malloc((size_t)n * sizeof(double));
+  double loss = NAN;
+  if (g && state && probs && ez) {
+    memcpy(g, gates, (size_t)num_gates * sizeof(orc_gate));
+    /* Circuit::set_parameters, circuit.rs:308-322: parametrised gates in order */
+    int64_t p = 0;
+    for (int64_t i = 0; i < num_gates && p < num_params; ++i)
+      if (is_parametrised(g[i].kind)) g[i].theta = params[p++];
+    orc_zero_state(state, n);
+    orc_forward(state, n, g, num_gates);
+    orc_measure(state, n, probs);
+    orc_expect_z(probs, n, ez);
+    loss = 0.;
+    for (int32_t q = 0; q < n; ++q) loss += weights[q] * ez[q];
+  }
+  free(g); free(state); free(probs); free(ez);
+  return loss;
+}
+
+void orc_param_shift_grad(int32_t n, const orc_gate* gates, int64_t num_gates,
+                          const double* params, int64_t num_params,
+                          const double* weights, double* grads) {
+  const double half_pi = 1.5707963267948966;
+  double* shifted = (double*)malloc((size_t)num_params * sizeof(double));
+  if (!shifted) return;
+  memcpy(shifted, params, (size_t)num_params * sizeof(double));
+  for (int64_t k = 0; k < num_params; ++k) {
+    shifted[k] = params[k] + half_pi;
+    double up = orc_loss(n, gates, num_gates, shifted, num_params, weights);
+    shifted[k] = params[k] - half_pi;
+    double down = orc_loss(n, gates, num_gates, shifted, num_params, weights);
+    shifted[k] = params[k];
+    grads[k] = 0.5 * (up - down);
+  }
+  free(shifted);
+}
+
+int32_t orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void orc_set_num_threads(int32_t t) {
+#ifdef _OPENMP
+  if (t > 0) omp_set_num_threads(t);
+#else
+  (void)t;
+#endif
+}

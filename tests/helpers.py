@@ -1,0 +1,73 @@
+"""Shared checks for the GPU parity tests.
+
+Tolerances (complex128): amplitudes and probabilities agree norm-wise,
+max|gpu - oracle| <= 1e-12 * max|oracle| (per-element relative error is
+undefined where amplitudes vanish); Pauli-Z expectations, which lie in
+[-1, 1], agree to 1e-12 absolute. Samples drawn from the same uniforms are
+identical except where u * total lies within 1e-12 of a CDF boundary.
+"""
+import ctypes
+
+import numpy as np
+
+AMP_RTOL = 1e-12
+EXPECT_ATOL = 1e-12
+BOUNDARY_ATOL = 1e-12
+
+
+def assert_state_close(got, want, rtol=AMP_RTOL, what="amplitudes"):
+    got = np.asarray(got)
+    want = np.asarray(want)
+    scale = max(np.max(np.abs(want)), 1e-300)
+    err = np.max(np.abs(got - want)) / scale
+    assert err <= rtol, f"{what}: normwise error {err:.3e} > {rtol:.0e}"
+    return err
+
+
+def assert_samples_match(probs, uniforms, got, oracle_mod):
+    ref = oracle_mod.sample(probs, uniforms)
+    got = np.asarray(got, dtype=np.uint64)
+    mism = np.nonzero(ref != got)[0]
+    if mism.size == 0:
+        return 0
+    cdf = np.concatenate([[0.0], np.cumsum(probs)])
+    for i in mism:
+        r, g = int(ref[i]), int(got[i])
+        assert r != 2 ** 64 - 1 and g != 2 ** 64 - 1, f"sample {i}: {r} vs {g}"
+        xsi = uniforms[i] * cdf[-1]
+        lo, hi = min(r, g), max(r, g)
+        gaps = np.abs(cdf[lo + 1:hi + 1] - xsi)
+        assert gaps.size and np.all(gaps <= BOUNDARY_ATOL), \
+            f"sample {i}: gpu {g} vs oracle {r}, xsi {xsi!r} not on a boundary (gap {gaps.min() if gaps.size else None})"
+    return int(mism.size)
+
+
+def random_state(n, rng):
+    v = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    return v / np.linalg.norm(v)
+
+
+def load_state(state_obj, psi):
+    from damavand_gb300._lib import check, dptr, lib
+    a = np.ascontiguousarray(psi, dtype=np.complex128)
+    check(lib.dmv_state_load_from_host_interleaved(state_obj.handle, dptr(a.view(np.float64))))
+
+
+def new_state(n, precision=0):
+    from damavand_gb300._lib import check, lib
+    from damavand_gb300.circuit import State
+    h = ctypes.c_void_p()
+    check(lib.dmv_state_create(n, precision, None, ctypes.byref(h)))
+    return State(h.value)
+
+
+def free_state(st):
+    from damavand_gb300._lib import lib
+    lib.dmv_state_destroy(st.handle)
+
+
+def apply_gates(st, gates, fusion=1):
+    from damavand_gb300._lib import check, lib
+    from damavand_gb300.workloads import gate_array
+    arr, count = gate_array(gates)
+    check(lib.dmv_apply_gates(st.handle, arr, count, fusion))
