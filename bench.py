@@ -45,6 +45,9 @@ UNIT = "gate-applies/s"
 # FP64 multiply-add throughput of a GB300 measured with an independent-FMA-chain kernel
 # (0.504 T FMA/s = 1.0 TFLOP/s); complex128 arithmetic is bounded by it.
 FP64_FMA_PEAK_T = 0.504
+# dram__bytes_read.sum + dram__bytes_write.sum per launch divided by the amplitudes of
+# the captured case (profiles/k_apply_window_c128_24q_full.md: 493.7 MB at 2^24).
+NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 493.698304e6 / (1 << 24)}
 
 
 def load_peaks():
@@ -300,13 +303,11 @@ def run_ours(args, world, rank, local):
     per_launch_bytes = d["bytes"] / max(d["launches"], 1)
     avg_launch_s = d["ms"] / max(d["launches"], 1) / 1e3
     achieved = per_launch_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
+    # DRAM bytes per launch from one ncu capture (profiles/*_full.md), scaled by state size.
     traffic = None
-    prof_path = os.path.join(REPO, "profiles", "traffic_per_launch.json")
-    if os.path.exists(prof_path):
-        try:
-            traffic = json.load(open(prof_path)).get(f"{dom}_n{n}")
-        except Exception:
-            traffic = None
+    key = (dom, "c128")
+    if key in NCU_TRAFFIC_PER_AMPLITUDE:
+        traffic = NCU_TRAFFIC_PER_AMPLITUDE[key] * (1 << n)
     roofline = {"bound": "hbm", "kernel": f"k_apply_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_launch_s * 1e3}

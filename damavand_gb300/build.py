@@ -71,9 +71,19 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")
+    _link_alias()
     if verbose:
         print(f"built {LIB_PATH}")
     return LIB_PATH
+
+
+def _link_alias() -> None:
+    """libdamavand-gpu.so -> libdamavand_gpu.so: the name the reference's build.rs
+    links (`cargo:rustc-link-lib=dylib=damavand-gpu`)."""
+    alias = os.path.join(PKG_DIR, "libdamavand-gpu.so")
+    if os.path.islink(alias) or os.path.exists(alias):
+        os.remove(alias)
+    os.symlink(LIB_NAME, alias)
 
 
 if __name__ == "__main__":
