@@ -79,6 +79,7 @@ SIGNATURES = {
     "dmv_sample": (ctypes.c_int, [_vp, _dp, _i64, _u64p]),
     "dmv_sample_probabilities": (ctypes.c_int, [_dp, _i64, _dp, _i64, _u64p]),
     "dmv_inner_product": (ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    "dmv_expect_z_noalloc": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),
     "dmv_adjoint_gradient": (ctypes.c_int, [_vp, ctypes.POINTER(Gate), _i64, _dp, _dp, _dp]),
     "dmv_circuit_create": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, _vpp]),
     "dmv_circuit_destroy": (ctypes.c_int, [_vp]),

@@ -171,6 +171,24 @@ int dmv_sample_probabilities(const double* probs, int64_t num_probs, const doubl
 /* <a|b> (conjugate-linear in a), FP64 accumulation. */
 int dmv_inner_product(dmv_state_t a, dmv_state_t b, double* re, double* im);
 
+/* Allocation-free <Z_q> for callers that must not let a library allocate
+ * device memory: code being captured into a CUDA graph (cudaMalloc is not
+ * allowed there), applications that hand all device memory out from their
+ * own pool, and loops that cannot take the device-wide synchronisation of
+ * cudaMalloc/cudaFree. It has no counterpart in the reference.
+ * `amps` are the caller's 2^num_qubits device amplitudes (interleaved, in
+ * `precision`); `out_device` receives num_qubits + 1 doubles on the device:
+ * <Z_0> ... <Z_{n-1}>, then the norm. Stream-ordered on `stream`. It calls
+ * no cudaMalloc/cudaFree: its partial sums live in one fixed device array
+ * compiled into the library (1216 x 35 doubles, 332.5 KiB, held on every GPU
+ * that loads the library until exit), hence num_qubits <= 34; larger sizes
+ * are rejected with DMV_ERR_INVALID. The first call on each device looks the
+ * array's device address up (and may load the library's device code): make
+ * it before any stream capture. Every call shares the array, so calls whose
+ * kernels overlap on the GPU race; serialise them. */
+int dmv_expect_z_noalloc(const void* amps, int32_t num_qubits, int32_t precision, double* out_device,
+                         void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Adjoint gradient                                                          */
 /* ------------------------------------------------------------------------ */
