@@ -42,9 +42,12 @@ sys.path.insert(0, REPO)
 
 METRIC = "30-qubit gate applies/s + HBM GB/s; adjoint vs param-shift grads/s at 1e-10"
 UNIT = "gate-applies/s"
+DTYPES = {"fp64": "f64 (complex128 storage and FP64 arithmetic)",
+          "fp32x2": "f32x2 (complex128 storage, FP32-pair arithmetic, ~48-bit)"}
 # FP64 multiply-add throughput of a GB300 measured with an independent-FMA-chain kernel
 # (0.504 T FMA/s = 1.0 TFLOP/s); complex128 arithmetic is bounded by it.
 FP64_FMA_PEAK_T = 0.504
+FP32_FMA_PEAK_T = 35.9
 # dram__bytes_read.sum + dram__bytes_write.sum per launch divided by the amplitudes of
 # the captured case (profiles/k_apply_window_c128_24q_full.md: 493.7 MB at 2^24).
 NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 493.698304e6 / (1 << 24)}
@@ -185,6 +188,7 @@ def workload_config(args, gates):
     return {"workload": f"{args.qubits}-qubit complex128 forward: H on all qubits + {args.layers} x "
                         f"[RX,RY,RZ per qubit; CNOT i->i+1], angles U[0,2pi) seed 1",
             "qubits": args.qubits, "gates": gates, "layers": args.layers, "precision": "complex128",
+            "arithmetic": args.arith,
             "fusion": "qubit windows" if not args.no_fusion else "none",
             "l2": "inputs larger than L2 (statevector 2^n x 16 B), no flush", "parallelism": "replicas"}
 
@@ -248,21 +252,25 @@ def adjoint_section(args):
             "loss": loss}
 
 
-def run_ours(args, world, rank, local):
+def read_families(lib, check):
     import ctypes
 
-    from damavand_gb300 import Circuit
-    from damavand_gb300._lib import (KERNEL_ADJOINT, KERNEL_REDUCE, KERNEL_SINGLE, KERNEL_WINDOW, check, dptr, lib)
-    from damavand_gb300.workloads import add_to_circuit, count, ladder_circuit, parameters
+    from damavand_gb300._lib import KERNEL_ADJOINT, KERNEL_REDUCE, KERNEL_SINGLE, KERNEL_WINDOW
+    fam = {}
+    for name, f in (("window", KERNEL_WINDOW), ("single", KERNEL_SINGLE), ("reduce", KERNEL_REDUCE),
+                    ("adjoint", KERNEL_ADJOINT)):
+        l, t, b, fm = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib.dmv_profile_read(f, ctypes.byref(l), ctypes.byref(t), ctypes.byref(b), ctypes.byref(fm)))
+        fam[name] = {"launches": l.value, "ms": t.value, "bytes": b.value, "arith_ops": fm.value}
+    return fam
 
-    check(lib.dmv_set_device(local))
-    n = args.qubits
-    gates = ladder_circuit(n, args.layers, seed=1)
-    G = count(gates)
-    c = Circuit(n, "gpu", fusion=not args.no_fusion)
-    add_to_circuit(c, gates)
+
+def timed_forward(c, args, world, local):
+    """W warm-up steps, then K steps between CUDA events on the library's stream (profiled)."""
+    import ctypes
+
+    from damavand_gb300._lib import check, lib
     st = c.state()
-    S = (1 << n) * 16
 
     def step():
         c.reset_amplitudes()
@@ -271,9 +279,6 @@ def run_ours(args, world, rank, local):
     for _ in range(args.warmup):
         step()
     st.synchronize()
-    passes, fused_ops, bytes_moved = c.plan_stats()
-
-    # ---- timed region: device-resident forward, CUDA events on the library's stream
     barrier(world)
     st.synchronize()
     lib.dmv_profile_reset()
@@ -289,14 +294,10 @@ def run_ours(args, world, rank, local):
     lib.dmv_profile_enable(0)
     barrier(world)
     step_ms = max_over_ranks(world, ms.value / args.steps)
-    value = world * G / (step_ms / 1e3)
+    return step_ms, read_families(lib, check), launches, clocks.summary(), step
 
-    fam = {}
-    for name, f in (("window", KERNEL_WINDOW), ("single", KERNEL_SINGLE), ("reduce", KERNEL_REDUCE),
-                    ("adjoint", KERNEL_ADJOINT)):
-        l, t, b, fm = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-        check(lib.dmv_profile_read(f, ctypes.byref(l), ctypes.byref(t), ctypes.byref(b), ctypes.byref(fm)))
-        fam[name] = {"launches": l.value, "ms": t.value, "bytes": b.value, "fp64_fma": fm.value}
+
+def rooflines(fam, n, arith):
     dom = max(fam, key=lambda k: fam[k]["ms"])
     d = fam[dom]
     peak, peak_kind = load_peaks()
@@ -305,19 +306,44 @@ def run_ours(args, world, rank, local):
     achieved = per_launch_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
     # DRAM bytes per launch from one ncu capture (profiles/*_full.md), scaled by state size.
     traffic = None
-    key = (dom, "c128")
-    if key in NCU_TRAFFIC_PER_AMPLITUDE:
-        traffic = NCU_TRAFFIC_PER_AMPLITUDE[key] * (1 << n)
+    if (dom, "c128") in NCU_TRAFFIC_PER_AMPLITUDE:
+        traffic = NCU_TRAFFIC_PER_AMPLITUDE[(dom, "c128")] * (1 << n)
     roofline = {"bound": "hbm", "kernel": f"k_apply_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_launch_s * 1e3}
-    # The same kernel against the FP64 multiply-add ceiling it actually meets on GB300.
-    fp64_rate = d["fp64_fma"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else 0.0
-    roofline_fp64 = {"bound": "fp64", "achieved": fp64_rate, "peak": FP64_FMA_PEAK_T, "unit": "T FMA/s",
-                     "frac": fp64_rate / FP64_FMA_PEAK_T,
-                     "peak_source": "measured (FP64 FMA chain kernel on this pool's GB300, 0.504 T FMA/s)"}
-    total_pass_bytes = sum(v["bytes"] for v in fam.values())
-    total_kernel_ms = sum(v["ms"] for v in fam.values())
+    # The same kernel against the arithmetic ceiling it meets on GB300: FP64
+    # multiply-adds for IEEE FP64 arithmetic, FP32 operations for FP32-pair arithmetic.
+    rate = d["arith_ops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else 0.0
+    if arith == "fp64":
+        ra = {"bound": "fp64", "achieved": rate, "peak": FP64_FMA_PEAK_T, "unit": "T FMA/s",
+              "frac": rate / FP64_FMA_PEAK_T, "peak_source": "measured (FP64 FMA chain kernel on this pool's GB300)"}
+    else:
+        ra = {"bound": "fp32", "achieved": rate, "peak": FP32_FMA_PEAK_T, "unit": "T op/s",
+              "frac": rate / FP32_FMA_PEAK_T, "peak_source": "measured (FP32 FMA chain kernel on this pool's GB300)"}
+    total_bytes = sum(v["bytes"] for v in fam.values())
+    total_ms = sum(v["ms"] for v in fam.values())
+    return roofline, ra, (total_bytes / (total_ms / 1e3) / 1e9 if total_ms else None)
+
+
+def run_ours(args, world, rank, local):
+    import ctypes
+
+    from damavand_gb300 import Circuit
+    from damavand_gb300._lib import check, dptr, lib
+    from damavand_gb300.workloads import add_to_circuit, count, ladder_circuit, parameters
+
+    check(lib.dmv_set_device(local))
+    n = args.qubits
+    gates = ladder_circuit(n, args.layers, seed=1)
+    G = count(gates)
+    S = (1 << n) * 16
+    c = Circuit(n, "gpu", fusion=not args.no_fusion, arithmetic=args.arith)
+    add_to_circuit(c, gates)
+    st = c.state()
+    step_ms, fam, launches, clocks, step = timed_forward(c, args, world, local)
+    value = world * G / (step_ms / 1e3)
+    passes, fused_ops, bytes_moved = c.plan_stats()
+    roofline, roofline_arith, pass_gbs = rooflines(fam, n, args.arith)
 
     # ---- e2e through the Circuit API with pinned host buffers
     params = parameters(gates)
@@ -328,12 +354,11 @@ def run_ours(args, world, rank, local):
     for a in (pin_params, re, im):
         if lib.dmv_host_register(a.ctypes.data, a.nbytes) == 0:
             registered.append(a)
-    h2d = pin_params.nbytes + G * ctypes.sizeof(ctypes.c_double) * 12  # parameters + uploaded op list
+    h2d = pin_params.nbytes + G * ctypes.sizeof(ctypes.c_double) * 20  # parameters + uploaded op list
     d2h = re.nbytes + im.nbytes
-    for _ in range(1):
-        c.set_parameters(pin_params)
-        step()
-        check(lib.dmv_state_copy_to_host(st.handle, dptr(re), dptr(im)))
+    c.set_parameters(pin_params)
+    step()
+    check(lib.dmv_state_copy_to_host(st.handle, dptr(re), dptr(im)))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -348,19 +373,40 @@ def run_ours(args, world, rank, local):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic (seeded angles, seed 1)",
+        "vs_baseline": None, "dtype": DTYPES[args.arith], "data": "synthetic (seeded angles, seed 1)",
         "config": workload_config(args, G),
-        "hbm_gbs_pass_bytes": total_pass_bytes / (total_kernel_ms / 1e3) / 1e9 if total_kernel_ms else None,
-        "per_gate_equiv_gbs": G * 2 * S * args.steps / (ms.value / 1e3) / 1e9,
+        "hbm_gbs_pass_bytes": pass_gbs,
+        "per_gate_equiv_gbs": G * 2 * S / (step_ms / 1e3) / 1e9,
         "plan": {"passes": passes, "fused_ops": fused_ops, "bytes_per_forward": bytes_moved},
         "kernels": fam,
         "roofline": roofline,
-        "roofline_fp64": roofline_fp64,
+        "roofline_arith": roofline_arith,
         "e2e": {"value": world * G / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
         "gpu_launches": int(launches),
-        "clocks": clocks.summary(),
+        "clocks": clocks,
     }
+
+    # ---- the other complex128 arithmetic, same workload and protocol, checked against this one
+    if not args.no_alt:
+        import torch
+        alt = "fp32x2" if args.arith == "fp64" else "fp64"
+        c2 = Circuit(n, "gpu", fusion=not args.no_fusion, arithmetic=alt)
+        add_to_circuit(c2, gates)
+        ms2, fam2, launches2, clocks2, _ = timed_forward(c2, args, world, local)
+        rl2, ra2, gbs2 = rooflines(fam2, n, alt)
+        ta, tb = c2.state().torch(), c.state().torch()  # both hold one forward from |0...0>
+        ref, other = (tb, ta) if args.arith == "fp64" else (ta, tb)
+        err = float(((other - ref).abs().max() / ref.abs().max()).item())
+        del ta, tb, ref, other
+        out["alt_arithmetic"] = {
+            "arithmetic": alt, "dtype": DTYPES[alt], "value": world * G / (ms2 / 1e3), "unit": UNIT,
+            "ms_per_step": ms2, "roofline": rl2, "roofline_arith": ra2, "hbm_gbs_pass_bytes": gbs2,
+            "gpu_launches": int(launches2), "clocks": clocks2,
+            "parity": {"against": "the FP64-arithmetic forward of this run", "normwise_max_err": err,
+                       "tolerance": 1e-12, "ok": err <= 1e-12}}
+        del c2
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = adjoint_section(args)
     if rank == 0 and not args.no_cpu:
@@ -377,6 +423,10 @@ def main():
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--no-fusion", action="store_true")
+    ap.add_argument("--no-alt", action="store_true",
+                    help="skip the second complex128 arithmetic (timed and checked against the first)")
+    ap.add_argument("--arith", choices=["fp64", "fp32x2"], default="fp64",
+                    help="complex128 arithmetic: IEEE FP64, or FP32 pairs (error-free transformations)")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -17,6 +17,7 @@ OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_NO_DEVICE, ERR_UNSUPPORTED, ERR_TIMEOUT,
 C128, C64 = 0, 1
 GATE_H, GATE_X, GATE_Y, GATE_Z, GATE_RX, GATE_RY, GATE_RZ, GATE_CNOT, GATE_MATRIX = range(9)
 FUSE_NONE, FUSE_WINDOW = 0, 1
+ARITH_FP64, ARITH_FP32X2 = 0, 1
 KERNEL_WINDOW, KERNEL_SINGLE, KERNEL_REDUCE, KERNEL_ADJOINT, KERNEL_OTHER = range(5)
 
 _ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_OOM: "out of memory", ERR_CUDA: "CUDA error",
@@ -64,6 +65,7 @@ SIGNATURES = {
     "dmv_state_info": (ctypes.c_int, [_vp, _i32p, _i32p, _i64p]),
     "dmv_state_set_zero": (ctypes.c_int, [_vp]),
     "dmv_state_synchronize": (ctypes.c_int, [_vp]),
+    "dmv_state_set_arithmetic": (ctypes.c_int, [_vp, _i32]),
     "dmv_state_device_ptr": (ctypes.c_int, [_vp, _vpp, _vpp]),
     "dmv_state_copy_to_host": (ctypes.c_int, [_vp, _dp, _dp]),
     "dmv_state_copy_to_host_interleaved": (ctypes.c_int, [_vp, _dp]),
@@ -81,6 +83,14 @@ SIGNATURES = {
     "dmv_inner_product": (ctypes.c_int, [_vp, _vp, _dp, _dp]),
     "dmv_expect_z_noalloc": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),
     "dmv_adjoint_gradient": (ctypes.c_int, [_vp, ctypes.POINTER(Gate), _i64, _dp, _dp, _dp]),
+    "dmv_batch_create": (ctypes.c_int, [_i32, _i32p, _i64p, ctypes.POINTER(Gate), _i32, _i32, _vpp]),
+    "dmv_batch_destroy": (ctypes.c_int, [_vp]),
+    "dmv_batch_configure": (ctypes.c_int, [_vp, _i32, _i32, _i32]),
+    "dmv_batch_autotune": (ctypes.c_int, [_vp, _i32p, _i32p, _i32p, _dp]),
+    "dmv_batch_run": (ctypes.c_int, [_vp, _dp]),
+    "dmv_batch_expect_z": (ctypes.c_int, [_vp, _dp]),
+    "dmv_batch_copy_state": (ctypes.c_int, [_vp, _i32, _dp]),
+    "dmv_batch_stats": (ctypes.c_int, [_vp, _i64p, _i64p, _i64p, _i32p, _dp]),
     "dmv_circuit_create": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, _vpp]),
     "dmv_circuit_destroy": (ctypes.c_int, [_vp]),
     "dmv_circuit_add_gate": (ctypes.c_int, [_vp, _i32, _i32, _i32, _f64, _i32]),
@@ -88,6 +98,7 @@ SIGNATURES = {
     "dmv_circuit_get_gate": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(Gate), _i32p]),
     "dmv_circuit_set_parameters": (ctypes.c_int, [_vp, _dp, _i64]),
     "dmv_circuit_set_fusion": (ctypes.c_int, [_vp, _i32]),
+    "dmv_circuit_set_arithmetic": (ctypes.c_int, [_vp, _i32]),
     "dmv_circuit_reset_amplitudes": (ctypes.c_int, [_vp]),
     "dmv_circuit_reset": (ctypes.c_int, [_vp]),
     "dmv_circuit_forward": (ctypes.c_int, [_vp]),

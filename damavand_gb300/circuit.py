@@ -74,7 +74,7 @@ class Circuit:
     """Quantum circuit on a GB300 statevector (drop-in for damavand.Circuit, apply_method="gpu")."""
 
     def __init__(self, num_qubits: int, apply_method: str | None = None, *, precision: str = "complex128",
-                 fusion: bool = True):
+                 fusion: bool = True, arithmetic: str = "fp64"):
         if precision not in _PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
         self.num_qubits = int(num_qubits)
@@ -86,6 +86,16 @@ class Circuit:
         self.precision = precision
         if not fusion:
             check(lib.dmv_circuit_set_fusion(self._h, _lib.FUSE_NONE))
+        self.set_arithmetic(arithmetic)
+
+    def set_arithmetic(self, arithmetic: str) -> None:
+        """'fp64' (IEEE FP64 multiply-adds) or 'fp32x2' (FP32-pair error-free arithmetic on
+        the complex128 amplitudes, ~1e-13 normwise on deep circuits); complex64 ignores it."""
+        modes = {"fp64": _lib.ARITH_FP64, "fp32x2": _lib.ARITH_FP32X2}
+        if arithmetic not in modes:
+            raise ValueError(f"arithmetic must be one of {sorted(modes)}")
+        check(lib.dmv_circuit_set_arithmetic(self._h, modes[arithmetic]))
+        self.arithmetic = arithmetic
 
     def __del__(self):
         h = getattr(self, "_h", None)

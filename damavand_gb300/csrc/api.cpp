@@ -380,6 +380,15 @@ extern "C" int dmv_state_set_zero(dmv_state_t s) {
   return launch_set_zero(s);
 }
 
+extern "C" int dmv_state_set_arithmetic(dmv_state_t s, int32_t arithmetic) {
+  clear_error();
+  DMV_TRY(check_state(s));
+  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2)
+    return set_error(DMV_ERR_INVALID, "unknown arithmetic %d", arithmetic);
+  s->arith = arithmetic;
+  return DMV_OK;
+}
+
 extern "C" int dmv_state_synchronize(dmv_state_t s) {
   clear_error();
   DMV_TRY(check_state(s));
@@ -736,6 +745,12 @@ extern "C" int dmv_circuit_set_fusion(dmv_circuit_t c, int32_t fusion) {
     return set_error(DMV_ERR_INVALID, "unknown fusion mode %d", fusion);
   c->fusion = fusion;
   return DMV_OK;
+}
+
+extern "C" int dmv_circuit_set_arithmetic(dmv_circuit_t c, int32_t arithmetic) {
+  clear_error();
+  DMV_TRY(check_circuit(c));
+  return dmv_state_set_arithmetic(c->state, arithmetic);
 }
 
 extern "C" int dmv_circuit_reset_amplitudes(dmv_circuit_t c) {

@@ -71,6 +71,14 @@ int32_t classify(const double m[8]) {
   return OP_GENERAL;
 }
 
+void split_matrix(Op& op) {
+  for (int i = 0; i < 8; ++i) {
+    const float hi = (float)op.m[i];
+    op.mh[i] = hi;
+    op.ml[i] = (float)(op.m[i] - (double)hi);
+  }
+}
+
 void matmul2(const double a[8], const double b[8], double out[8]) {
   double r[8];
   for (int i = 0; i < 2; ++i)
@@ -150,6 +158,7 @@ Op make_op(const PGate& g, int32_t target_pos, int32_t ctrl, int32_t ctrl_kind) 
   Op op;
   std::memset(&op, 0, sizeof(op));
   std::memcpy(op.m, g.m, sizeof(op.m));
+  split_matrix(op);
   op.target = target_pos;
   op.ctrl = ctrl;
   op.ctrl_kind = ctrl_kind;
@@ -205,7 +214,7 @@ int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
   };
 
   const int32_t k = std::min(opt.tile_bits, n);
-  if (opt.fusion == DMV_FUSE_NONE || k < 2) {
+  if (!opt.windows_only && (opt.fusion == DMV_FUSE_NONE || k < 2)) {
     for (const PGate& g : fg) emit_single(g);
     return DMV_OK;
   }
@@ -252,7 +261,7 @@ int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
       pending.erase(pending.begin());
       continue;
     }
-    if (take.size() == 1) {
+    if (take.size() == 1 && !opt.windows_only) {
       emit_single(fg[(size_t)take.front()]);
     } else {
       Pass ps;

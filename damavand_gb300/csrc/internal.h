@@ -65,9 +65,11 @@ enum CtrlKind : int32_t {
   CTRL_GLOBAL = 2   // control qubit is outside the tile: constant per tile
 };
 
-// One operation as the kernels see it (64-byte aligned, 96 bytes).
+// One operation as the kernels see it (160 bytes).
 struct alignas(16) Op {
   double m[8];        // row-major 2x2, (re, im) pairs
+  float mh[8];        // m split into FP32 pairs: m = mh + ml (FP32-pair arithmetic)
+  float ml[8];
   int32_t target;     // local bit (fused) or qubit (unfused)
   int32_t ctrl;       // local bit or global qubit, per ctrl_kind
   int32_t ctrl_kind;  // CtrlKind
@@ -76,7 +78,16 @@ struct alignas(16) Op {
   int32_t generator;  // 0 none, 1 X, 2 Y, 3 Z: generator of a rotation (adjoint)
   int32_t pad[2];
 };
-static_assert(sizeof(Op) == 96, "Op layout");
+static_assert(sizeof(Op) == 160, "Op layout");
+
+// Fills op.mh / op.ml from op.m (hi = nearest float, lo = nearest float of the rest).
+void split_matrix(Op& op);
+
+// Arithmetic used for complex128 storage.
+enum Arith : int32_t {
+  ARITH_FP64 = 0,    // IEEE FP64 multiply-adds
+  ARITH_FP32X2 = 1   // FP32-pair (double-float) error-free transformations
+};
 
 // Host-side gate after parsing.
 struct Gate {
@@ -124,6 +135,7 @@ struct PlanOptions {
   int32_t fusion = DMV_FUSE_WINDOW;
   int32_t tile_bits = 12;  // log2 amplitudes per tile
   int32_t low_bits = 6;    // always-local low qubits (coalesced chunks)
+  bool windows_only = false;  // every pass a window pass (the batched kernel runs only those)
 };
 
 int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
@@ -145,6 +157,7 @@ struct dmv_state_s {
   int32_t n = 0;
   int64_t N = 0;
   int32_t precision = DMV_C128;
+  int32_t arith = dmv::ARITH_FP64;  // complex128 arithmetic (ignored for complex64)
   int device = 0;
   void* amps = nullptr;
   cudaStream_t stream = nullptr;
@@ -178,4 +191,17 @@ int launch_adjoint_step(dmv_state_s* psi, dmv_state_s* lam, const Op& op, double
 int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const double* weights,
                      double* loss, double* grads);
 int upload_ops(dmv_state_s* s, const Op* ops, int64_t count);
+
+// Chunk-mass / Pauli-Z reduction into caller-provided device buffers:
+// `mass` holds num_chunks doubles, `partial` partial_elems, `sums` n+1
+// (mass with bit q set for q < n, then the total).
+struct ChunkMassShape {
+  int chunk_bits;
+  int64_t num_chunks;
+  int grid;
+  int64_t partial_elems;
+};
+ChunkMassShape chunk_mass_shape(int n);
+int launch_chunk_mass_into(const void* src, int src_kind, int n, double* mass, double* partial, double* sums,
+                           cudaStream_t stream);
 }  // namespace dmv

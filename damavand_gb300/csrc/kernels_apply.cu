@@ -14,8 +14,8 @@
 //    tile is constant over the tile and is tested once per tile.
 #include <algorithm>
 
-#include "complex_ops.cuh"
 #include "internal.h"
+#include "policies.cuh"
 
 namespace dmv {
 
@@ -35,11 +35,10 @@ int num_sms() {
   return sms;
 }
 
-template <typename R, int CLS, bool CTRL>
+template <typename P, int CLS, bool CTRL>
 __global__ void __launch_bounds__(kSingleThreads)
-k_apply_single(typename VecOf<R>::T* __restrict__ a, int64_t num_pairs, int target, int control,
-               M2<R> m) {
-  using V = typename VecOf<R>::T;
+k_apply_single(typename P::G* __restrict__ a, int64_t num_pairs, int target, int control, const typename P::Mat m) {
+  using T = typename P::T;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int lo = CTRL ? min(target, control) : target;
   const int hi = CTRL ? max(target, control) : target;
@@ -51,42 +50,46 @@ k_apply_single(typename VecOf<R>::T* __restrict__ a, int64_t num_pairs, int targ
       i0 = insert_zero(j, target);
     }
     const int64_t i1 = i0 | (int64_t(1) << target);
-    V a0 = a[i0];
-    V a1 = a[i1];
-    apply_pair<R, CLS>(m, a0, a1);
-    a[i0] = a0;
-    a[i1] = a1;
+    if constexpr (CLS == OP_SWAP) {
+      const typename P::G g0 = a[i0];
+      a[i0] = a[i1];
+      a[i1] = g0;
+    } else {
+      T a0 = P::in(a[i0]);
+      T a1 = P::in(a[i1]);
+      P::template apply<CLS>(m, a0, a1);
+      a[i0] = P::out(a0);
+      a[i1] = P::out(a1);
+    }
   }
 }
 
-template <typename R, int CLS, bool CTRL>
-void launch_single_t(typename VecOf<R>::T* a, int32_t n, const Op& op, cudaStream_t stream) {
+template <typename P, int CLS, bool CTRL>
+void launch_single_t(typename P::G* a, int32_t n, const Op& op, cudaStream_t stream) {
   const int64_t pairs = (int64_t(1) << n) >> (CTRL ? 2 : 1);
   const int64_t want = (pairs + kSingleThreads - 1) / kSingleThreads;
   const int64_t cap = (int64_t)num_sms() * 16;
   const int grid = (int)std::max<int64_t>(1, std::min(want, cap));
-  k_apply_single<R, CLS, CTRL><<<grid, kSingleThreads, 0, stream>>>(a, pairs, op.target, op.ctrl,
-                                                                     to_m2<R>(op.m));
+  k_apply_single<P, CLS, CTRL><<<grid, kSingleThreads, 0, stream>>>(a, pairs, op.target, op.ctrl, P::mat(op));
 }
 
-template <typename R, int CLS>
-void launch_single_c(typename VecOf<R>::T* a, int32_t n, const Op& op, cudaStream_t stream) {
+template <typename P, int CLS>
+void launch_single_c(typename P::G* a, int32_t n, const Op& op, cudaStream_t stream) {
   if (op.ctrl_kind != CTRL_NONE && op.ctrl >= 0)
-    launch_single_t<R, CLS, true>(a, n, op, stream);
+    launch_single_t<P, CLS, true>(a, n, op, stream);
   else
-    launch_single_t<R, CLS, false>(a, n, op, stream);
+    launch_single_t<P, CLS, false>(a, n, op, stream);
 }
 
-template <typename R>
+template <typename P>
 void launch_single(void* amps, int32_t n, const Op& op, cudaStream_t stream) {
-  using V = typename VecOf<R>::T;
-  V* a = static_cast<V*>(amps);
+  typename P::G* a = static_cast<typename P::G*>(amps);
   switch (op.cls) {
-    case OP_SWAP: launch_single_c<R, OP_SWAP>(a, n, op, stream); break;
-    case OP_DIAG: launch_single_c<R, OP_DIAG>(a, n, op, stream); break;
-    case OP_ANTI: launch_single_c<R, OP_ANTI>(a, n, op, stream); break;
-    case OP_REAL: launch_single_c<R, OP_REAL>(a, n, op, stream); break;
-    default: launch_single_c<R, OP_GENERAL>(a, n, op, stream); break;
+    case OP_SWAP: launch_single_c<P, OP_SWAP>(a, n, op, stream); break;
+    case OP_DIAG: launch_single_c<P, OP_DIAG>(a, n, op, stream); break;
+    case OP_ANTI: launch_single_c<P, OP_ANTI>(a, n, op, stream); break;
+    case OP_REAL: launch_single_c<P, OP_REAL>(a, n, op, stream); break;
+    default: launch_single_c<P, OP_GENERAL>(a, n, op, stream); break;
   }
 }
 
@@ -100,42 +103,16 @@ struct WindowParams {
   const Op* ops;
 };
 
-template <typename R, int CLS, typename V>
-__device__ __forceinline__ void tile_op(V* tile, int T, const Op& op, const M2<R>& m) {
-  const int t = op.target;
-  if (op.ctrl_kind == CTRL_LOCAL) {
-    const int c = op.ctrl;
-    const int lo = min(t, c), hi = max(t, c);
-    for (int q = threadIdx.x; q < (T >> 2); q += blockDim.x) {
-      const uint32_t l0 = insert_zero32(insert_zero32((uint32_t)q, lo), hi) | (1u << c);
-      const uint32_t l1 = l0 | (1u << t);
-      V a0 = tile[l0], a1 = tile[l1];
-      apply_pair<R, CLS>(m, a0, a1);
-      tile[l0] = a0;
-      tile[l1] = a1;
-    }
-  } else {
-    for (int q = threadIdx.x; q < (T >> 1); q += blockDim.x) {
-      const uint32_t l0 = insert_zero32((uint32_t)q, t);
-      const uint32_t l1 = l0 | (1u << t);
-      V a0 = tile[l0], a1 = tile[l1];
-      apply_pair<R, CLS>(m, a0, a1);
-      tile[l0] = a0;
-      tile[l1] = a1;
-    }
-  }
-}
-
 __device__ __forceinline__ int64_t spread_high(uint32_t h, const WindowParams& p) {
   int64_t off = 0;
   for (int i = 0; i < p.nh; ++i) off |= (int64_t)((h >> i) & 1u) << p.high[i];
   return off;
 }
 
-template <typename R>
+template <typename P>
 __global__ void __launch_bounds__(kWindowThreads)
-k_apply_window(typename VecOf<R>::T* __restrict__ a, const WindowParams p) {
-  using V = typename VecOf<R>::T;
+k_apply_window(typename P::G* __restrict__ a, const WindowParams p) {
+  using V = typename P::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tile = reinterpret_cast<V*>(smem_raw);
   const int T = 1 << p.k;
@@ -144,30 +121,18 @@ k_apply_window(typename VecOf<R>::T* __restrict__ a, const WindowParams p) {
     int64_t base = tix << p.low;
     for (int i = 0; i < p.nh; ++i) base = insert_zero(base, p.high[i]);
     for (int l = threadIdx.x; l < T; l += blockDim.x)
-      tile[l] = a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)];
+      tile[l] = P::in(a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)]);
     __syncthreads();
-    for (int o = 0; o < p.num_ops; ++o) {
-      const Op& op = p.ops[o];
-      if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1)) continue;  // uniform per tile
-      const M2<R> m = to_m2<R>(op.m);
-      switch (op.cls) {
-        case OP_SWAP: tile_op<R, OP_SWAP>(tile, T, op, m); break;
-        case OP_DIAG: tile_op<R, OP_DIAG>(tile, T, op, m); break;
-        case OP_ANTI: tile_op<R, OP_ANTI>(tile, T, op, m); break;
-        case OP_REAL: tile_op<R, OP_REAL>(tile, T, op, m); break;
-        default: tile_op<R, OP_GENERAL>(tile, T, op, m); break;
-      }
-      __syncthreads();
-    }
+    tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base);
     for (int l = threadIdx.x; l < T; l += blockDim.x)
-      a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)] = tile[l];
+      a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)] = P::out(tile[l]);
     __syncthreads();
   }
 }
 
-template <typename R>
+template <typename P>
 int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cudaStream_t stream) {
-  using V = typename VecOf<R>::T;
+  using V = typename P::T;
   WindowParams p;
   p.k = ps.low_bits + ps.num_high;
   p.low = ps.low_bits;
@@ -179,16 +144,15 @@ int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cuda
   const size_t smem = (size_t(1) << p.k) * sizeof(V);
   static size_t configured = 0;
   if (smem > configured) {
-    DMV_CUDA_TRY(cudaFuncSetAttribute(k_apply_window<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    DMV_CUDA_TRY(cudaFuncSetAttribute(k_apply_window<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 48 * 1024)));
     configured = smem;
   }
   int per_sm = 0;
-  DMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_window<R>,
-                                                             kWindowThreads, smem));
+  DMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_window<P>, kWindowThreads, smem));
   if (per_sm < 1) return set_error(DMV_ERR_CUDA, "window kernel cannot fit %zu bytes of shared memory", smem);
   const int64_t grid = std::min<int64_t>(p.num_tiles, (int64_t)per_sm * num_sms());
-  k_apply_window<R><<<(int)grid, kWindowThreads, smem, stream>>>(static_cast<V*>(amps), p);
+  k_apply_window<P><<<(int)grid, kWindowThreads, smem, stream>>>(static_cast<typename P::G*>(amps), p);
   return DMV_OK;
 }
 
@@ -202,14 +166,17 @@ int upload_ops(dmv_state_s* s, const Op* ops, int64_t count) {
   return DMV_OK;
 }
 
-// Multiply-adds one op performs over the whole statevector: GENERAL 16 per
-// amplitude pair, REAL / DIAG / ANTI 8, SWAP none; a control halves it.
-double op_multiply_adds(const Op& op, int64_t N) {
+// Arithmetic operations one op performs over the whole statevector. FP64 /
+// FP32 storage arithmetic: multiply-adds, GENERAL 16 per amplitude pair,
+// REAL / DIAG / ANTI 8, SWAP none. FP32-pair arithmetic: FP32 operations of
+// the compensated dot products, 172 per pair (four 4-term dots) and 76 (four
+// 2-term dots). A control halves the count.
+double op_multiply_adds(const Op& op, int64_t N, bool pair_arith) {
   double per_pair = 0.;
   switch (op.cls) {
-    case OP_GENERAL: per_pair = 16.; break;
+    case OP_GENERAL: per_pair = pair_arith ? 172. : 16.; break;
     case OP_SWAP: per_pair = 0.; break;
-    default: per_pair = 8.; break;
+    default: per_pair = pair_arith ? 76. : 8.; break;
   }
   const double pairs = (double)N / 2.0;
   return per_pair * pairs * (op.ctrl_kind != CTRL_NONE ? 0.5 : 1.0);
@@ -222,21 +189,24 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   const Op* ops_dev = static_cast<const Op*>(s->ops_dev.ptr);
   int64_t bytes = 0;
   const int64_t S = (int64_t)s->amp_bytes();
+  const bool pair = s->precision == DMV_C128 && s->arith == ARITH_FP32X2;
   for (const Pass& ps : plan.passes) {
     if (ps.kind == 0) {
       const Op& op = plan.ops[(size_t)ps.op_begin];
       const int64_t b = op.ctrl_kind != CTRL_NONE ? S : 2 * S;
-      const int64_t tok = prof_begin(DMV_KERNEL_SINGLE, s->stream, (double)b, op_multiply_adds(op, s->N));
-      if (s->precision == DMV_C128) launch_single<double>(s->amps, s->n, op, s->stream);
-      else launch_single<float>(s->amps, s->n, op, s->stream);
+      const int64_t tok = prof_begin(DMV_KERNEL_SINGLE, s->stream, (double)b, op_multiply_adds(op, s->N, pair));
+      if (s->precision == DMV_C64) launch_single<PolF32>(s->amps, s->n, op, s->stream);
+      else if (s->arith == ARITH_FP32X2) launch_single<PolDF>(s->amps, s->n, op, s->stream);
+      else launch_single<PolF64>(s->amps, s->n, op, s->stream);
       prof_end(tok, s->stream);
       bytes += b;
     } else {
       double fmas = 0.;
-      for (int64_t o = 0; o < ps.op_count; ++o) fmas += op_multiply_adds(plan.ops[(size_t)(ps.op_begin + o)], s->N);
+      for (int64_t o = 0; o < ps.op_count; ++o) fmas += op_multiply_adds(plan.ops[(size_t)(ps.op_begin + o)], s->N, pair);
       const int64_t tok = prof_begin(DMV_KERNEL_WINDOW, s->stream, (double)(2 * S), fmas);
-      if (s->precision == DMV_C128) DMV_TRY(launch_window<double>(s->amps, s->n, ps, ops_dev, s->stream));
-      else DMV_TRY(launch_window<float>(s->amps, s->n, ps, ops_dev, s->stream));
+      if (s->precision == DMV_C64) DMV_TRY(launch_window<PolF32>(s->amps, s->n, ps, ops_dev, s->stream));
+      else if (s->arith == ARITH_FP32X2) DMV_TRY(launch_window<PolDF>(s->amps, s->n, ps, ops_dev, s->stream));
+      else DMV_TRY(launch_window<PolF64>(s->amps, s->n, ps, ops_dev, s->stream));
       prof_end(tok, s->stream);
       bytes += 2 * S;
     }

@@ -397,6 +397,29 @@ int run_sampler(const void* src, int src_kind, int chunk_bits, int64_t num_chunk
 
 }  // namespace
 
+ChunkMassShape chunk_mass_shape(int n) {
+  ChunkMassShape sh;
+  sh.chunk_bits = chunk_bits_for(n);
+  sh.num_chunks = int64_t(1) << (n - sh.chunk_bits);
+  sh.grid = grid_for_chunks(sh.num_chunks);
+  sh.partial_elems = (int64_t)sh.grid * (n + 1);
+  return sh;
+}
+
+int launch_chunk_mass_into(const void* src, int src_kind, int n, double* mass, double* partial, double* sums,
+                           cudaStream_t stream) {
+  const ChunkMassShape sh = chunk_mass_shape(n);
+  switch (src_kind) {
+    case 0: k_chunk_mass<0><<<sh.grid, kRedThreads, 0, stream>>>(src, n, sh.chunk_bits, sh.num_chunks, mass, partial); break;
+    case 1: k_chunk_mass<1><<<sh.grid, kRedThreads, 0, stream>>>(src, n, sh.chunk_bits, sh.num_chunks, mass, partial); break;
+    default: k_chunk_mass<2><<<sh.grid, kRedThreads, 0, stream>>>(src, n, sh.chunk_bits, sh.num_chunks, mass, partial); break;
+  }
+  k_reduce_partials<<<1, 64, 0, stream>>>(partial, n + 1, sh.grid, sums);
+  count_launch(2);
+  DMV_CUDA_TRY(cudaGetLastError());
+  return DMV_OK;
+}
+
 int launch_probabilities(dmv_state_s* s, double* probs_device) {
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((s->N + kRedThreads - 1) / kRedThreads,
                                                                (int64_t)sm_count() * 16));
@@ -589,6 +612,7 @@ int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const doubl
       Op op;
       std::memset(&op, 0, sizeof(op));
       adjoint2(g.m, op.m);
+      split_matrix(op);
       op.target = g.target;
       op.ctrl = g.control;
       op.ctrl_kind = g.control >= 0 ? CTRL_GLOBAL : CTRL_NONE;

@@ -71,6 +71,19 @@ def random_circuit(n: int, depth: int, rng: np.random.Generator, controlled_rota
     return gates
 
 
+def uneven_batch(count: int = 512, seed: int = 4, min_qubits: int = 10, max_qubits: int = 22,
+                 min_depth: int = 5, max_depth: int = 40):
+    """The batched configuration: `count` random circuits with qubit counts uniform in
+    [min_qubits, max_qubits] and depths uniform in [min_depth, max_depth], all from `seed`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.integers(min_qubits, max_qubits + 1))
+        depth = int(rng.integers(min_depth, max_depth + 1))
+        out.append((n, random_circuit(n, depth, rng)))
+    return out
+
+
 def parameters(gates) -> np.ndarray:
     return np.array([g[4] for g in gates if g[0] in PARAMETRISED and not g[3]], dtype=np.float64)
 
