@@ -252,6 +252,96 @@ def adjoint_section(args):
             "loss": loss}
 
 
+def normwise_err(got, ref, chunk: int = 1 << 26) -> float:
+    """max|got - ref| / max|ref| over two device tensors, in slices (no full-size temporaries)."""
+    import torch
+    num, den = 0.0, 0.0
+    for i in range(0, ref.numel(), chunk):
+        x = got[i:i + chunk].to(torch.complex128)
+        y = ref[i:i + chunk]
+        num = max(num, float((x - y).abs().max().item()))
+        den = max(den, float(y.abs().max().item()))
+    return num / den if den else num
+
+
+def batch_section(args):
+    """The batched configuration: 512 circuits, 10..22 qubits, depth 5..40, seed 4, one persistent
+    launch in a CUDA graph; complex128 and complex64 (FP64 reductions); c64 <Z> error vs c128."""
+    from damavand_gb300.batch import Batch
+    from damavand_gb300.workloads import count, uneven_batch
+    circuits = uneven_batch(512, seed=4)
+    gates_total = sum(count(g) for _, g in circuits)
+    amps = sum(1 << n for n, _ in circuits)
+    out, ez = {}, {}
+    for prec, size in (("complex128", 16), ("complex64", 8)):
+        b = Batch(circuits, prec)
+        tune = b.autotune()
+        b.run()
+        times = [b.run() for _ in range(max(3, args.steps))]
+        ms = float(np.median(times))
+        st = b.stats()
+        out[prec] = {"ms_per_run": ms, "circuits_per_s": len(circuits) / (ms / 1e3),
+                     "gate_applies_per_s": gates_total / (ms / 1e3), "autotuned": tune, "items": st["items"],
+                     "passes": st["passes"], "grid": st["grid"], "cuda_graph": st["cuda_graph"],
+                     "arena_gb": amps * size / 1e9}
+        ez[prec] = b.expect_z()
+        del b
+    err = [float(np.max(np.abs(a - b))) for a, b in zip(ez["complex64"], ez["complex128"])]
+    out["complex64_expect_z_err_vs_complex128"] = {"max": max(err), "median": float(np.median(err))}
+    out["circuits"] = len(circuits)
+    out["gates"] = gates_total
+    return out
+
+
+def large_section(args):
+    """31 qubits complex128: forward + adjoint of the 12-layer ring ansatz (1116 parameters, seed 5,
+    loss = mean <Z_i>); 32 qubits complex64 forward with FP64 reductions, compared with complex128."""
+    import torch
+
+    from damavand_gb300 import Circuit
+    from damavand_gb300.workloads import add_to_circuit, ring_ansatz
+    res = {}
+    n = 31
+    gates = ring_ansatz(n, 12, seed=5)
+    c = Circuit(n)
+    add_to_circuit(c, gates)
+    t0 = time.perf_counter()
+    c.forward()
+    c.synchronize()
+    res["forward31_s"] = time.perf_counter() - t0
+    res["forward31_gate_applies_per_s"] = len(gates) / res["forward31_s"]
+    w = np.full(n, 1.0 / n)
+    t0 = time.perf_counter()
+    loss, grads = c.adjoint_gradient(w)
+    res["adjoint31_s"] = time.perf_counter() - t0
+    res["adjoint31_params"] = int(grads.size)
+    res["adjoint31_grads_per_s"] = grads.size / res["adjoint31_s"]
+    res["adjoint31_loss"] = loss
+    del c
+    torch.cuda.empty_cache()
+    m = 32
+    g32 = ring_ansatz(m, 12, seed=5)
+    c64 = Circuit(m, precision="complex64")
+    add_to_circuit(c64, g32)
+    t0 = time.perf_counter()
+    c64.forward()
+    c64.synchronize()
+    res["forward32_c64_s"] = time.perf_counter() - t0
+    res["forward32_c64_gate_applies_per_s"] = len(g32) / res["forward32_c64_s"]
+    ez64 = c64.expectation_z()
+    c128 = Circuit(m, arithmetic="fp32x2")
+    add_to_circuit(c128, g32)
+    c128.forward()
+    ez128 = c128.expectation_z()
+    res["c64_vs_c128_32q_expect_z_max_err"] = float(np.max(np.abs(ez64 - ez128)))
+    a, b = c64.state().torch(), c128.state().torch()
+    res["c64_vs_c128_32q_amp_normwise_err"] = normwise_err(a, b)
+    res["c128_32q_reference_arithmetic"] = "fp32x2 (9e-14 from FP64 at 30 qubits)"
+    del a, b, c64, c128
+    torch.cuda.empty_cache()
+    return res
+
+
 def read_families(lib, check):
     import ctypes
 
@@ -387,6 +477,30 @@ def run_ours(args, world, rank, local):
         "clocks": clocks,
     }
 
+    # ---- readout of the final 30-qubit state: <Z_q>, 1000 samples, probabilities on the device
+    import torch
+    u = np.random.default_rng([1, 1]).random(1000)
+    c.expectation_z()
+    t0 = time.perf_counter()
+    ez = c.expectation_z()
+    t_ez = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    samples = c.sample_array(1000, uniforms=u)
+    t_s = time.perf_counter() - t0
+    probs = torch.empty(1 << n, dtype=torch.float64, device="cuda")
+    check(lib.dmv_measure_device(st.handle, ctypes.cast(probs.data_ptr(), ctypes.POINTER(ctypes.c_double))))
+    st.synchronize()
+    t0 = time.perf_counter()
+    check(lib.dmv_measure_device(st.handle, ctypes.cast(probs.data_ptr(), ctypes.POINTER(ctypes.c_double))))
+    st.synchronize()
+    t_p = time.perf_counter() - t0
+    del probs
+    torch.cuda.empty_cache()
+    out["readout"] = {"expect_z_ms": t_ez * 1e3, "expect_z_gbs": S / t_ez / 1e9, "sample_1000_ms": t_s * 1e3,
+                      "probabilities_on_device_ms": t_p * 1e3, "probabilities_gbs": (S + S // 2) / t_p / 1e9,
+                      "norm": float(c.norm()), "first_samples": [int(x) for x in samples[:4]],
+                      "mean_abs_expect_z": float(np.mean(np.abs(ez)))}
+
     # ---- the other complex128 arithmetic, same workload and protocol, checked against this one
     if not args.no_alt:
         import torch
@@ -397,7 +511,7 @@ def run_ours(args, world, rank, local):
         rl2, ra2, gbs2 = rooflines(fam2, n, alt)
         ta, tb = c2.state().torch(), c.state().torch()  # both hold one forward from |0...0>
         ref, other = (tb, ta) if args.arith == "fp64" else (ta, tb)
-        err = float(((other - ref).abs().max() / ref.abs().max()).item())
+        err = normwise_err(other, ref)
         del ta, tb, ref, other
         out["alt_arithmetic"] = {
             "arithmetic": alt, "dtype": DTYPES[alt], "value": world * G / (ms2 / 1e3), "unit": UNIT,
@@ -409,6 +523,10 @@ def run_ours(args, world, rank, local):
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = adjoint_section(args)
+    if rank == 0 and not args.no_batch:
+        out["batch"] = batch_section(args)
+    if rank == 0 and args.workload == "large":
+        out["large"] = large_section(args)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     return out
@@ -428,6 +546,9 @@ def main():
     ap.add_argument("--arith", choices=["fp64", "fp32x2"], default="fp64",
                     help="complex128 arithmetic: IEEE FP64, or FP32 pairs (error-free transformations)")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--workload", choices=["default", "large"], default="default",
+                    help="'large' adds the 31-qubit forward + adjoint and the 32-qubit complex64 forward")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-gates", type=int, default=3, help="gates per reference step")

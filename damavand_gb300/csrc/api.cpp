@@ -96,9 +96,21 @@ void prof_end(int64_t token, cudaStream_t stream) {
   if (token < (int64_t)g_prof.size()) cudaEventRecord(g_prof[(size_t)token].b, stream);
 }
 
+namespace {
+std::atomic<int32_t> g_fail_allocs{0};
+}
+
+bool injected_alloc_failure() {
+  int32_t v = g_fail_allocs.load();
+  while (v > 0)
+    if (g_fail_allocs.compare_exchange_weak(v, v - 1)) return true;
+  return false;
+}
+
 int DeviceBuffer::reserve(size_t n) {
   if (n <= bytes && ptr) return DMV_OK;
   release();
+  if (injected_alloc_failure()) return set_error(DMV_ERR_OOM, "cudaMalloc(%zu) failed: injected failure", n);
   void* p = nullptr;
   const cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 256));
   if (e != cudaSuccess) {
@@ -159,6 +171,23 @@ int launch_join(void* amps, int precision, int64_t offset, int64_t count, const 
 namespace dmv {
 namespace {
 
+// Device address of page-locked (cudaHostRegister'ed or cudaMallocHost'ed)
+// host memory, or nullptr for ordinary pageable memory.
+void* mapped_device_pointer(const void* host) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (attr.type != cudaMemoryTypeHost) return nullptr;
+  void* dev = nullptr;
+  if (cudaHostGetDevicePointer(&dev, const_cast<void*>(host), 0) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return dev;
+}
+
 int copy_out(dmv_state_s* s, double* re, double* im, double* inter) {
   const int64_t chunk = std::min<int64_t>(s->N, kStageAmps);
   // Fast path: complex128 interleaved output is a straight copy.
@@ -166,6 +195,17 @@ int copy_out(dmv_state_s* s, double* re, double* im, double* inter) {
     DMV_CUDA_TRY(cudaMemcpyAsync(inter, s->amps, s->amp_bytes(), cudaMemcpyDeviceToHost, s->stream));
     DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return DMV_OK;
+  }
+  // Page-locked host buffers: the split kernel writes them directly over the link.
+  {
+    double* dre = re ? static_cast<double*>(mapped_device_pointer(re)) : nullptr;
+    double* dim = im ? static_cast<double*>(mapped_device_pointer(im)) : nullptr;
+    double* dint = inter ? static_cast<double*>(mapped_device_pointer(inter)) : nullptr;
+    if ((inter && dint) || (!inter && dre && dim)) {
+      DMV_TRY(launch_split(s->amps, s->precision, 0, s->N, dre, dim, dint, s->stream));
+      DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
+      return DMV_OK;
+    }
   }
   DeviceBuffer stage;
   DMV_TRY(stage.reserve((size_t)chunk * 2 * sizeof(double)));
@@ -201,6 +241,16 @@ int copy_in(dmv_state_s* s, const double* re, const double* im, const double* in
     DMV_CUDA_TRY(cudaMemcpyAsync(s->amps, inter, s->amp_bytes(), cudaMemcpyHostToDevice, s->stream));
     DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return DMV_OK;
+  }
+  {
+    const double* dre = re ? static_cast<const double*>(mapped_device_pointer(re)) : nullptr;
+    const double* dim = im ? static_cast<const double*>(mapped_device_pointer(im)) : nullptr;
+    const double* dint = inter ? static_cast<const double*>(mapped_device_pointer(inter)) : nullptr;
+    if ((inter && dint) || (!inter && dre && dim)) {
+      DMV_TRY(launch_join(s->amps, s->precision, 0, s->N, dre, dim, dint, s->stream));
+      DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
+      return DMV_OK;
+    }
   }
   DeviceBuffer stage;
   DMV_TRY(stage.reserve((size_t)chunk * 2 * sizeof(double)));
@@ -248,6 +298,11 @@ extern "C" int dmv_last_error(void) { return dmv::last_error(); }
 extern "C" const char* dmv_last_error_string(void) { return dmv::g_last_msg; }
 extern "C" const char* dmv_version(void) { return "damavand_gb300 0.1.0 (sm_103a)"; }
 extern "C" int64_t dmv_kernel_launch_count(void) { return dmv::g_launches.load(); }
+
+extern "C" int dmv_debug_fail_allocations(int32_t count) {
+  dmv::g_fail_allocs.store(count > 0 ? count : 0);
+  return DMV_OK;
+}
 
 extern "C" int dmv_set_device(int32_t device) {
   clear_error();
@@ -321,7 +376,7 @@ extern "C" int dmv_state_create(int32_t num_qubits, int32_t precision, void* str
   s->N = int64_t(1) << num_qubits;
   s->precision = precision;
   cudaGetDevice(&s->device);
-  const cudaError_t e = cudaMalloc(&s->amps, s->amp_bytes());
+  const cudaError_t e = injected_alloc_failure() ? cudaErrorMemoryAllocation : cudaMalloc(&s->amps, s->amp_bytes());
   if (e != cudaSuccess) {
     cudaGetLastError();
     delete s;

@@ -25,7 +25,7 @@ namespace dmv {
 namespace {
 
 constexpr int kBatchThreads = 512;
-constexpr long long kSpinLimit = 1LL << 22;  // x 1 us sleeps: ~4 s before giving up
+constexpr long long kDefaultSpinLimit = 1LL << 22;  // x 1 us sleeps: ~4 s before giving up
 
 struct BatchPass {
   int32_t k, low, nh, num_ops;
@@ -52,7 +52,7 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 template <typename P>
 __global__ void __launch_bounds__(kBatchThreads)
 k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes, const BatchItem* __restrict__ items,
-        int64_t num_items, const Op* __restrict__ ops, unsigned long long* counters) {
+        int64_t num_items, const Op* __restrict__ ops, unsigned long long* counters, long long spin_limit) {
   using V = typename P::T;
   using G = typename P::G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -68,7 +68,7 @@ k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes,
         const unsigned long long need = (unsigned long long)items[it].wait_count;
         long long spins = 0;
         while (ld_acquire_u64(done) < need) {
-          if (++spins > kSpinLimit || *(volatile unsigned long long*)&counters[1] != 0ull) {
+          if (++spins > spin_limit || *(volatile unsigned long long*)&counters[1] != 0ull) {
             stop = 2;
             break;
           }
@@ -147,6 +147,8 @@ struct dmv_batch_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool use_graph = true;
+  long long spin_limit = kDefaultSpinLimit;
+  bool poison_next_plan = false;  // test hook: one item waits for a count that never arrives
   int grid = 0;
   float last_ms = 0.f;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -217,6 +219,15 @@ int batch_plan(dmv_batch_s* b) {
       items_done_before[(size_t)c] += made;
     }
   }
+  if (b->poison_next_plan) {
+    // Test hook: the last dependent item waits for more completions than its
+    // circuit will ever report, so its bounded wait must run out.
+    for (size_t i = items.size(); i-- > 0;)
+      if (items[i].wait_count > 0) {
+        items[i].wait_count = int64_t(1) << 60;
+        break;
+      }
+  }
   b->num_items = (int64_t)items.size();
   b->num_passes = (int64_t)passes.size();
   b->num_ops = (int64_t)ops.size();
@@ -258,7 +269,7 @@ int batch_launch_kernel(dmv_batch_s* b) {
                                   static_cast<const BatchPass*>(b->passes_dev.ptr),
                                   static_cast<const BatchItem*>(b->items_dev.ptr), b->num_items,
                                   static_cast<const Op*>(b->ops_dev.ptr),
-                                  static_cast<unsigned long long*>(b->counters_dev.ptr)));
+                                  static_cast<unsigned long long*>(b->counters_dev.ptr), b->spin_limit));
   count_launch();
   return DMV_OK;
 }
@@ -380,7 +391,7 @@ extern "C" int dmv_batch_create(int32_t num_circuits, const int32_t* num_qubits,
   b->total_amps = off;
   int rc = DMV_OK;
   do {
-    if (cudaMalloc(&b->arena, (size_t)b->total_amps * b->amp_size()) != cudaSuccess) {
+    if (injected_alloc_failure() || cudaMalloc(&b->arena, (size_t)b->total_amps * b->amp_size()) != cudaSuccess) {
       cudaGetLastError();
       b->arena = nullptr;
       rc = set_error(DMV_ERR_OOM, "cannot allocate the %.2f GB batch arena", (double)b->total_amps * b->amp_size() / 1e9);
@@ -446,6 +457,15 @@ extern "C" int dmv_batch_configure(dmv_batch_t b, int32_t tile_bits, int32_t low
   b->opt.tile_bits = tile_bits;
   b->opt.low_bits = low_bits;
   b->tiles_per_item = tiles_per_item;
+  destroy_graph(b);
+  return batch_plan(b);
+}
+
+extern "C" int dmv_batch_debug_wait_limit(dmv_batch_t b, int64_t spin_limit, int32_t poison) {
+  clear_error();
+  if (!b || spin_limit < 1) return set_error(DMV_ERR_INVALID, "bad wait limit");
+  b->spin_limit = spin_limit;
+  b->poison_next_plan = poison != 0;
   destroy_graph(b);
   return batch_plan(b);
 }

@@ -40,6 +40,10 @@ int last_error();
 // Counts the library's own kernel launches (reported by the benchmark).
 void count_launch(int64_t n = 1);
 
+// Test hook (dmv_debug_fail_allocations): true when this device allocation
+// must fail as if the device were out of memory.
+bool injected_alloc_failure();
+
 // Optional per-launch CUDA-event profiling (dmv_profile_*). prof_begin
 // returns a token (or -1 when profiling is off); prof_end closes it.
 int64_t prof_begin(int family, cudaStream_t stream, double algorithmic_bytes, double multiply_adds = 0.0);

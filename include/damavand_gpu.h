@@ -233,6 +233,13 @@ int dmv_batch_expect_z(dmv_batch_t b, double* out);
 int dmv_batch_copy_state(dmv_batch_t b, int32_t index, double* interleaved);
 int dmv_batch_stats(dmv_batch_t b, int64_t* items, int64_t* passes, int64_t* ops, int32_t* grid,
                     double* last_ms);
+/* Test hook: sets the dependency-wait limit (iterations of ~1 us) and, with
+ * poison != 0, re-plans so one item waits for a count that never arrives; the
+ * next run must then end with DMV_ERR_TIMEOUT instead of hanging. */
+int dmv_batch_debug_wait_limit(dmv_batch_t b, int64_t spin_limit, int32_t poison);
+/* Test hook: the next `count` device allocations of the library fail (as if
+ * out of memory). */
+int dmv_debug_fail_allocations(int32_t count);
 
 /* ------------------------------------------------------------------------ */
 /* Circuit front-end (the reference's pyo3 Circuit, src/qubit_backend/circuit.rs:78-770) */

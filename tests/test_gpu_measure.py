@@ -182,6 +182,43 @@ def test_legacy_abi_round_trip(built_lib):
     assert lib.dmv_last_error() == 1
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_host_copies_pageable_and_registered(built_lib, precision):
+    """Split-layout copies through the staged path (pageable) and the direct path (registered)."""
+    from damavand_gb300._lib import check, dptr, lib
+    n = 21
+    rng = np.random.default_rng(77)
+    psi = random_state(n, rng)
+    if precision == 1:
+        psi = psi.astype(np.complex64).astype(np.complex128)
+    st = new_state(n, precision)
+    try:
+        load_state(st, psi)
+        for registered in (False, True):
+            re, im = np.empty(1 << n), np.empty(1 << n)
+            if registered:
+                check(lib.dmv_host_register(re.ctypes.data, re.nbytes))
+                check(lib.dmv_host_register(im.ctypes.data, im.nbytes))
+            try:
+                check(lib.dmv_state_copy_to_host(st.handle, dptr(re), dptr(im)))
+                np.testing.assert_array_equal(re + 1j * im, psi)
+                re2, im2 = re[::-1].copy(), im[::-1].copy()
+                if registered:
+                    re[:] = re2
+                    im[:] = im2
+                    check(lib.dmv_state_load_from_host(st.handle, dptr(re), dptr(im)))
+                else:
+                    check(lib.dmv_state_load_from_host(st.handle, dptr(re2), dptr(im2)))
+                np.testing.assert_array_equal(st.numpy(), re2 + 1j * im2)
+                load_state(st, psi)
+            finally:
+                if registered:
+                    lib.dmv_host_unregister(re.ctypes.data)
+                    lib.dmv_host_unregister(im.ctypes.data)
+    finally:
+        free_state(st)
+
+
 def test_torch_view_zero_copy(built_lib):
     torch = pytest.importorskip("torch")
     from damavand_gb300 import Circuit
