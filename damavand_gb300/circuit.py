@@ -89,9 +89,10 @@ class Circuit:
         self.set_arithmetic(arithmetic)
 
     def set_arithmetic(self, arithmetic: str) -> None:
-        """'fp64' (IEEE FP64 multiply-adds) or 'fp32x2' (FP32-pair error-free arithmetic on
-        the complex128 amplitudes, ~1e-13 normwise on deep circuits); complex64 ignores it."""
-        modes = {"fp64": _lib.ARITH_FP64, "fp32x2": _lib.ARITH_FP32X2}
+        """Arithmetic on the complex128 amplitudes (complex64 ignores it): 'fp64' (IEEE FP64
+        multiply-adds), 'fp32x2' (FP32-pair error-free arithmetic, ~1e-13 normwise on deep
+        circuits) or 'int64' (block fixed point with exact integer products)."""
+        modes = {"fp64": _lib.ARITH_FP64, "fp32x2": _lib.ARITH_FP32X2, "int64": _lib.ARITH_INT64}
         if arithmetic not in modes:
             raise ValueError(f"arithmetic must be one of {sorted(modes)}")
         check(lib.dmv_circuit_set_arithmetic(self._h, modes[arithmetic]))

@@ -282,8 +282,7 @@ int copy_in(dmv_state_s* s, const double* re, const double* im, const double* in
 
 int apply_gate_list(dmv_state_s* s, const std::vector<Gate>& gates, int32_t fusion) {
   Plan plan;
-  PlanOptions opt;
-  opt.fusion = fusion;
+  const PlanOptions opt = plan_options_for(s, fusion);
   DMV_TRY(build_plan(gates, s->n, s->precision, opt, plan));
   return launch_plan(s, plan);
 }
@@ -438,7 +437,7 @@ extern "C" int dmv_state_set_zero(dmv_state_t s) {
 extern "C" int dmv_state_set_arithmetic(dmv_state_t s, int32_t arithmetic) {
   clear_error();
   DMV_TRY(check_state(s));
-  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2)
+  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2 && arithmetic != DMV_ARITH_INT64)
     return set_error(DMV_ERR_INVALID, "unknown arithmetic %d", arithmetic);
   s->arith = arithmetic;
   return DMV_OK;
@@ -549,6 +548,38 @@ extern "C" int dmv_apply_gates(dmv_state_t s, const dmv_gate_t* gates, int64_t n
   std::vector<Gate> parsed;
   DMV_TRY(parse_gates(gates, num_gates, s->n, parsed));
   return apply_gate_list(s, parsed, fusion);
+}
+
+extern "C" int dmv_plan_describe(int32_t num_qubits, int32_t precision, const dmv_gate_t* gates, int64_t num_gates,
+                                 int32_t fusion, int32_t tile_bits, int64_t* num_passes, int64_t* num_window_passes,
+                                 int64_t* num_ops, int32_t* max_local_qubits) {
+  clear_error();
+  if (num_qubits < 1 || num_qubits > 34) return set_error(DMV_ERR_INVALID, "num_qubits %d outside [1, 34]", num_qubits);
+  if (precision != DMV_C128 && precision != DMV_C64) return set_error(DMV_ERR_INVALID, "unknown precision");
+  if (fusion != DMV_FUSE_NONE && fusion != DMV_FUSE_WINDOW) return set_error(DMV_ERR_INVALID, "unknown fusion mode");
+  if (tile_bits < 0 || tile_bits > 13) return set_error(DMV_ERR_INVALID, "tile_bits %d outside [0, 13]", tile_bits);
+  std::vector<Gate> parsed;
+  DMV_TRY(parse_gates(gates, num_gates, num_qubits, parsed));
+  dmv_state_s probe;
+  probe.n = num_qubits;
+  probe.precision = precision;
+  PlanOptions opt = plan_options_for(&probe, fusion);
+  if (tile_bits > 0) opt.tile_bits = tile_bits;
+  Plan plan;
+  DMV_TRY(build_plan(parsed, num_qubits, precision, opt, plan));
+  int64_t windows = 0;
+  int32_t max_local = 0;
+  for (const Pass& p : plan.passes) {
+    if (p.kind == 1) {
+      ++windows;
+      max_local = std::max(max_local, p.low_bits + p.num_high);
+    }
+  }
+  if (num_passes) *num_passes = (int64_t)plan.passes.size();
+  if (num_window_passes) *num_window_passes = windows;
+  if (num_ops) *num_ops = (int64_t)plan.ops.size();
+  if (max_local_qubits) *max_local_qubits = max_local;
+  return DMV_OK;
 }
 
 namespace {

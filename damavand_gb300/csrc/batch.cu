@@ -50,7 +50,7 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 // counters[0]: queue head, counters[1]: error flag, counters[2 + b]: items of
 // circuit b completed.
 template <typename P>
-__global__ void __launch_bounds__(kBatchThreads)
+__global__ void __launch_bounds__(kBatchThreads, 2)
 k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes, const BatchItem* __restrict__ items,
         int64_t num_items, const Op* __restrict__ ops, unsigned long long* counters, long long spin_limit) {
   using V = typename P::T;
@@ -59,6 +59,9 @@ k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes,
   V* tile = reinterpret_cast<V*>(smem_raw);
   __shared__ long long s_item;
   __shared__ int s_stop;
+  __shared__ int64_t s_slot[kMaxSlots];
+  __shared__ int s_red[kTileThreads / 32];
+  (void)s_red;
   for (;;) {
     if (threadIdx.x == 0) {
       const long long it = (long long)atomicAdd(&counters[0], 1ull);
@@ -85,24 +88,23 @@ k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes,
     const BatchPass ps = passes[item.pass];
     G* a = arena + ps.amp_offset;
     const int T = 1 << ps.k;
-    const uint32_t lowmask = (1u << ps.low) - 1u;
+    const int64_t t_off = tile_thread_offset(ps.low, ps.nh, ps.high);
+    tile_slot_offsets(ps.low, ps.nh, ps.high, (T + kTileThreads - 1) >> kTileThreadBits, s_slot);
+    __syncthreads();
     for (int64_t tix = item.tile_begin; tix < item.tile_end; ++tix) {
       int64_t base = tix << ps.low;
       for (int i = 0; i < ps.nh; ++i) base = insert_zero(base, ps.high[i]);
-      for (int l = threadIdx.x; l < T; l += blockDim.x) {
-        int64_t off = 0;
-        const uint32_t h = (uint32_t)l >> ps.low;
-        for (int i = 0; i < ps.nh; ++i) off |= (int64_t)((h >> i) & 1u) << ps.high[i];
-        // L2-coherent load: another SM wrote this amplitude in the previous pass.
-        tile[l] = P::in(__ldcg(a + (base | (int64_t)(l & lowmask) | off)));
-      }
-      __syncthreads();
-      tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
-      for (int l = threadIdx.x; l < T; l += blockDim.x) {
-        int64_t off = 0;
-        const uint32_t h = (uint32_t)l >> ps.low;
-        for (int i = 0; i < ps.nh; ++i) off |= (int64_t)((h >> i) & 1u) << ps.high[i];
-        a[base | (int64_t)(l & lowmask) | off] = P::out(tile[l]);
+      // L2-coherent loads: another SM wrote these amplitudes in the previous pass.
+      if constexpr (P::kBlockScaled) {
+        const int e = tile_load_fx<true>(tile, a, base, T, t_off, s_slot, s_red);
+        __syncthreads();
+        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
+        tile_store_fx(tile, a, base, T, t_off, s_slot, e);
+      } else {
+        tile_load<P, true>(tile, a, base, T, t_off, s_slot);
+        __syncthreads();
+        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
+        tile_store<P>(tile, a, base, T, t_off, s_slot);
       }
       __syncthreads();
     }
@@ -147,6 +149,7 @@ struct dmv_batch_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool use_graph = true;
+  bool all_unitary = true;  // block fixed point needs unitary ops everywhere
   long long spin_limit = kDefaultSpinLimit;
   bool poison_next_plan = false;  // test hook: one item waits for a count that never arrives
   int grid = 0;
@@ -228,6 +231,8 @@ int batch_plan(dmv_batch_s* b) {
         break;
       }
   }
+  b->all_unitary = true;
+  for (const Op& op : ops) b->all_unitary = b->all_unitary && op.unitary;
   b->num_items = (int64_t)items.size();
   b->num_passes = (int64_t)passes.size();
   b->num_ops = (int64_t)ops.size();
@@ -291,6 +296,7 @@ int batch_enqueue(dmv_batch_s* b) {
   if (b->num_items > 0) {
     if (b->precision == DMV_C64) DMV_TRY(batch_launch_kernel<PolF32>(b));
     else if (b->arith == ARITH_FP32X2) DMV_TRY(batch_launch_kernel<PolDF>(b));
+    else if (b->arith == ARITH_INT64 && b->all_unitary) DMV_TRY(batch_launch_kernel<PolFX>(b));
     else DMV_TRY(batch_launch_kernel<PolF64>(b));
   }
   double* red = static_cast<double*>(b->reduce_dev.ptr);
@@ -355,7 +361,8 @@ extern "C" int dmv_batch_create(int32_t num_circuits, const int32_t* num_qubits,
   *out = nullptr;
   if (num_circuits < 1 || !num_qubits || !gate_offsets) return set_error(DMV_ERR_INVALID, "empty batch");
   if (precision != DMV_C128 && precision != DMV_C64) return set_error(DMV_ERR_INVALID, "unknown precision");
-  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2) return set_error(DMV_ERR_INVALID, "unknown arithmetic");
+  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2 && arithmetic != DMV_ARITH_INT64)
+    return set_error(DMV_ERR_INVALID, "unknown arithmetic");
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
     cudaGetLastError();
@@ -450,7 +457,7 @@ extern "C" int dmv_batch_destroy(dmv_batch_t b) {
 extern "C" int dmv_batch_configure(dmv_batch_t b, int32_t tile_bits, int32_t low_bits, int32_t tiles_per_item) {
   clear_error();
   if (!b) return set_error(DMV_ERR_INVALID, "null batch");
-  if (tile_bits < 2 || tile_bits > 13 || low_bits < 1 || low_bits > tile_bits || tiles_per_item < 1)
+  if (tile_bits < 2 || tile_bits > 13 || low_bits < 1 || low_bits > tile_bits || low_bits > 9 || tiles_per_item < 1)
     return set_error(DMV_ERR_INVALID, "bad batch configuration (%d, %d, %d)", tile_bits, low_bits, tiles_per_item);
   if (b->precision == DMV_C128 && tile_bits > 12)
     return set_error(DMV_ERR_INVALID, "complex128 tiles hold at most 2^12 amplitudes");

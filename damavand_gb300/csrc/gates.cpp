@@ -72,11 +72,30 @@ int32_t classify(const double m[8]) {
 }
 
 void split_matrix(Op& op) {
+  bool bounded = true;
   for (int i = 0; i < 8; ++i) {
     const float hi = (float)op.m[i];
     op.mh[i] = hi;
     op.ml[i] = (float)(op.m[i] - (double)hi);
+    if (!(std::fabs(op.m[i]) <= 1.0)) bounded = false;
+    const long long f = bounded ? std::llround(std::ldexp(op.m[i], 54)) : 0;  // |f| <= 2^54
+    op.fh[i] = (int32_t)(f >> 31);
+    op.fl[i] = (int32_t)(f & 0x7FFFFFFFll);
   }
+  // U^dagger U = I to 1e-12: the fixed-point headroom argument needs unitarity.
+  double worst = bounded ? 0.0 : 1.0;
+  for (int r = 0; r < 2 && bounded; ++r)
+    for (int c = 0; c < 2; ++c) {
+      double re = 0., im = 0.;
+      for (int k = 0; k < 2; ++k) {  // sum_k conj(m[k][r]) m[k][c]
+        const double ar = op.m[2 * (2 * k + r)], ai = -op.m[2 * (2 * k + r) + 1];
+        const double br = op.m[2 * (2 * k + c)], bi = op.m[2 * (2 * k + c) + 1];
+        re += ar * br - ai * bi;
+        im += ar * bi + ai * br;
+      }
+      worst = std::max(worst, std::fabs(re - (r == c ? 1.0 : 0.0)) + std::fabs(im));
+    }
+  op.unitary = worst <= 1e-12 ? 1 : 0;
 }
 
 void matmul2(const double a[8], const double b[8], double out[8]) {

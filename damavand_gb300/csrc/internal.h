@@ -69,28 +69,33 @@ enum CtrlKind : int32_t {
   CTRL_GLOBAL = 2   // control qubit is outside the tile: constant per tile
 };
 
-// One operation as the kernels see it (160 bytes).
+// One operation as the kernels see it (224 bytes).
 struct alignas(16) Op {
   double m[8];        // row-major 2x2, (re, im) pairs
   float mh[8];        // m split into FP32 pairs: m = mh + ml (FP32-pair arithmetic)
   float ml[8];
+  int32_t fh[8];      // m as Q.54 fixed point: round(m * 2^54) = fh * 2^31 + fl, fl in [0, 2^31)
+  int32_t fl[8];
   int32_t target;     // local bit (fused) or qubit (unfused)
   int32_t ctrl;       // local bit or global qubit, per ctrl_kind
   int32_t ctrl_kind;  // CtrlKind
   int32_t cls;        // OpClass
   int32_t param;      // index of the gradient slot (adjoint) or -1
   int32_t generator;  // 0 none, 1 X, 2 Y, 3 Z: generator of a rotation (adjoint)
-  int32_t pad[2];
+  int32_t unitary;    // 1 when m is unitary to 1e-12 (block fixed point relies on it)
+  int32_t pad;
 };
-static_assert(sizeof(Op) == 160, "Op layout");
+static_assert(sizeof(Op) == 224, "Op layout");
 
-// Fills op.mh / op.ml from op.m (hi = nearest float, lo = nearest float of the rest).
+// Fills op.mh / op.ml (FP32 pair: hi = nearest float, lo = nearest float of
+// the rest), op.fh / op.fl (Q.54 limbs) and op.unitary from op.m.
 void split_matrix(Op& op);
 
 // Arithmetic used for complex128 storage.
 enum Arith : int32_t {
   ARITH_FP64 = 0,    // IEEE FP64 multiply-adds
-  ARITH_FP32X2 = 1   // FP32-pair (double-float) error-free transformations
+  ARITH_FP32X2 = 1,  // FP32-pair (double-float) error-free transformations
+  ARITH_INT64 = 2    // int64 block fixed point on the integer pipe
 };
 
 // Host-side gate after parsing.
@@ -179,6 +184,16 @@ struct dmv_state_s {
 
 namespace dmv {
 int ensure_pinned(dmv_state_s* s, size_t bytes);
+
+// Planner settings for a state: complex64 tiles hold 2^13 amplitudes (64 KB of
+// shared memory, like a 2^12 complex128 tile), so each HBM pass covers one
+// more qubit.
+inline PlanOptions plan_options_for(const dmv_state_s* s, int32_t fusion) {
+  PlanOptions opt;
+  opt.fusion = fusion;
+  opt.tile_bits = s->precision == DMV_C64 ? 13 : 12;
+  return opt;
+}
 
 // Kernel launchers (kernels_*.cu). All stream-ordered on s->stream.
 int launch_set_zero(dmv_state_s* s);

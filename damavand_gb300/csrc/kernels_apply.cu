@@ -54,6 +54,14 @@ k_apply_single(typename P::G* __restrict__ a, int64_t num_pairs, int target, int
       const typename P::G g0 = a[i0];
       a[i0] = a[i1];
       a[i1] = g0;
+    } else if constexpr (P::kBlockScaled) {
+      const typename P::G g0 = a[i0], g1 = a[i1];
+      const int e = P::pair_exponent(g0, g1);
+      T a0 = P::in(g0, e);
+      T a1 = P::in(g1, e);
+      P::template apply<CLS>(m, a0, a1);
+      a[i0] = P::out(a0, e);
+      a[i1] = P::out(a1, e);
     } else {
       T a0 = P::in(a[i0]);
       T a1 = P::in(a[i1]);
@@ -103,29 +111,35 @@ struct WindowParams {
   const Op* ops;
 };
 
-__device__ __forceinline__ int64_t spread_high(uint32_t h, const WindowParams& p) {
-  int64_t off = 0;
-  for (int i = 0; i < p.nh; ++i) off |= (int64_t)((h >> i) & 1u) << p.high[i];
-  return off;
-}
+static_assert(kWindowThreads == kTileThreads, "tile staging assumes 512 threads");
 
 template <typename P>
-__global__ void __launch_bounds__(kWindowThreads)
+__global__ void __launch_bounds__(kWindowThreads, 2)
 k_apply_window(typename P::G* __restrict__ a, const WindowParams p) {
   using V = typename P::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int64_t s_slot[kMaxSlots];
   V* tile = reinterpret_cast<V*>(smem_raw);
   const int T = 1 << p.k;
-  const uint32_t lowmask = (1u << p.low) - 1u;
+  const int64_t t_off = tile_thread_offset(p.low, p.nh, p.high);
+  tile_slot_offsets(p.low, p.nh, p.high, (T + kTileThreads - 1) >> kTileThreadBits, s_slot);
+  __syncthreads();
+  __shared__ int s_red[kTileThreads / 32];
   for (int64_t tix = blockIdx.x; tix < p.num_tiles; tix += gridDim.x) {
     int64_t base = tix << p.low;
     for (int i = 0; i < p.nh; ++i) base = insert_zero(base, p.high[i]);
-    for (int l = threadIdx.x; l < T; l += blockDim.x)
-      tile[l] = P::in(a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)]);
-    __syncthreads();
-    tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base);
-    for (int l = threadIdx.x; l < T; l += blockDim.x)
-      a[base | (int64_t)(l & lowmask) | spread_high((uint32_t)l >> p.low, p)] = P::out(tile[l]);
+    if constexpr (P::kBlockScaled) {
+      const int e = tile_load_fx<false>(tile, a, base, T, t_off, s_slot, s_red);
+      __syncthreads();
+      tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base);
+      tile_store_fx(tile, a, base, T, t_off, s_slot, e);
+    } else {
+      (void)s_red;
+      tile_load<P, false>(tile, a, base, T, t_off, s_slot);
+      __syncthreads();
+      tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base);
+      tile_store<P>(tile, a, base, T, t_off, s_slot);
+    }
     __syncthreads();
   }
 }
@@ -171,12 +185,15 @@ int upload_ops(dmv_state_s* s, const Op* ops, int64_t count) {
 // REAL / DIAG / ANTI 8, SWAP none. FP32-pair arithmetic: FP32 operations of
 // the compensated dot products, 172 per pair (four 4-term dots) and 76 (four
 // 2-term dots). A control halves the count.
-double op_multiply_adds(const Op& op, int64_t N, bool pair_arith) {
+// INT64 block fixed point: IMAD.WIDE limb products, 64 per pair (four 4-term
+// sums of 4 limb products each) and 32.
+double op_multiply_adds(const Op& op, int64_t N, int arith) {
   double per_pair = 0.;
+  const bool pair_arith = arith == ARITH_FP32X2, fixed = arith == ARITH_INT64;
   switch (op.cls) {
-    case OP_GENERAL: per_pair = pair_arith ? 172. : 16.; break;
+    case OP_GENERAL: per_pair = pair_arith ? 172. : fixed ? 64. : 16.; break;
     case OP_SWAP: per_pair = 0.; break;
-    default: per_pair = pair_arith ? 76. : 8.; break;
+    default: per_pair = pair_arith ? 76. : fixed ? 32. : 8.; break;
   }
   const double pairs = (double)N / 2.0;
   return per_pair * pairs * (op.ctrl_kind != CTRL_NONE ? 0.5 : 1.0);
@@ -189,23 +206,30 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   const Op* ops_dev = static_cast<const Op*>(s->ops_dev.ptr);
   int64_t bytes = 0;
   const int64_t S = (int64_t)s->amp_bytes();
-  const bool pair = s->precision == DMV_C128 && s->arith == ARITH_FP32X2;
   for (const Pass& ps : plan.passes) {
+    // Block fixed point needs unitary ops; a pass with any other op runs in FP64.
+    int arith = s->precision == DMV_C64 ? ARITH_FP64 : s->arith;
+    if (arith == ARITH_INT64)
+      for (int64_t o = 0; o < ps.op_count; ++o)
+        if (!plan.ops[(size_t)(ps.op_begin + o)].unitary) arith = ARITH_FP64;
     if (ps.kind == 0) {
       const Op& op = plan.ops[(size_t)ps.op_begin];
       const int64_t b = op.ctrl_kind != CTRL_NONE ? S : 2 * S;
-      const int64_t tok = prof_begin(DMV_KERNEL_SINGLE, s->stream, (double)b, op_multiply_adds(op, s->N, pair));
+      const int64_t tok = prof_begin(DMV_KERNEL_SINGLE, s->stream, (double)b, op_multiply_adds(op, s->N, arith));
       if (s->precision == DMV_C64) launch_single<PolF32>(s->amps, s->n, op, s->stream);
-      else if (s->arith == ARITH_FP32X2) launch_single<PolDF>(s->amps, s->n, op, s->stream);
+      else if (arith == ARITH_FP32X2) launch_single<PolDF>(s->amps, s->n, op, s->stream);
+      else if (arith == ARITH_INT64) launch_single<PolFX>(s->amps, s->n, op, s->stream);
       else launch_single<PolF64>(s->amps, s->n, op, s->stream);
       prof_end(tok, s->stream);
       bytes += b;
     } else {
       double fmas = 0.;
-      for (int64_t o = 0; o < ps.op_count; ++o) fmas += op_multiply_adds(plan.ops[(size_t)(ps.op_begin + o)], s->N, pair);
+      for (int64_t o = 0; o < ps.op_count; ++o)
+        fmas += op_multiply_adds(plan.ops[(size_t)(ps.op_begin + o)], s->N, arith);
       const int64_t tok = prof_begin(DMV_KERNEL_WINDOW, s->stream, (double)(2 * S), fmas);
       if (s->precision == DMV_C64) DMV_TRY(launch_window<PolF32>(s->amps, s->n, ps, ops_dev, s->stream));
-      else if (s->arith == ARITH_FP32X2) DMV_TRY(launch_window<PolDF>(s->amps, s->n, ps, ops_dev, s->stream));
+      else if (arith == ARITH_FP32X2) DMV_TRY(launch_window<PolDF>(s->amps, s->n, ps, ops_dev, s->stream));
+      else if (arith == ARITH_INT64) DMV_TRY(launch_window<PolFX>(s->amps, s->n, ps, ops_dev, s->stream));
       else DMV_TRY(launch_window<PolF64>(s->amps, s->n, ps, ops_dev, s->stream));
       prof_end(tok, s->stream);
       bytes += 2 * S;

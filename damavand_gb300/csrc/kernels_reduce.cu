@@ -11,6 +11,7 @@
 
 #include "complex_ops.cuh"
 #include "internal.h"
+#include "policies.cuh"
 
 namespace dmv {
 
@@ -295,13 +296,15 @@ k_scale_z(V* __restrict__ dst, const V* __restrict__ src, int64_t N, const doubl
 // One step of the adjoint sweep for gate U (op holds U^dagger):
 //   grad += Im <lam| P |psi>   (P the rotation's generator, pre-update values)
 //   psi <- U^dagger psi, lam <- U^dagger lam.
-template <typename R>
+// The state updates use the state's arithmetic policy (FP64, FP32, FP32-pair);
+// the gradient term is always accumulated in FP64 from the loaded values.
+template <typename P>
 __global__ void __launch_bounds__(kRedThreads)
-k_adjoint_step(typename VecOf<R>::T* __restrict__ psi, typename VecOf<R>::T* __restrict__ lam,
+k_adjoint_step(typename P::G* __restrict__ psi, typename P::G* __restrict__ lam,
                int64_t num_pairs, Op op, int apply, double* __restrict__ partial) {
-  using V = typename VecOf<R>::T;
+  using V = typename P::G;
   __shared__ double red[32];
-  const M2<R> m = to_m2<R>(op.m);
+  const typename P::Mat m = P::dmat(op);
   const int t = op.target;
   const bool ctrl = op.ctrl_kind != CTRL_NONE && op.ctrl >= 0;
   const int c = op.ctrl;
@@ -325,10 +328,20 @@ k_adjoint_step(typename VecOf<R>::T* __restrict__ psi, typename VecOf<R>::T* __r
       }
     }
     if (apply) {
-      apply_pair_dyn<R>(op.cls, m, p0, p1);
-      apply_pair_dyn<R>(op.cls, m, l0, l1);
-      psi[i0] = p0; psi[i1] = p1;
-      lam[i0] = l0; lam[i1] = l1;
+      if constexpr (P::kBlockScaled) {  // each pair is its own block
+        const int ep = P::pair_exponent(p0, p1), el = P::pair_exponent(l0, l1);
+        typename P::T q0 = P::in(p0, ep), q1 = P::in(p1, ep), m0 = P::in(l0, el), m1 = P::in(l1, el);
+        apply_dyn<P>(op.cls, m, q0, q1);
+        apply_dyn<P>(op.cls, m, m0, m1);
+        psi[i0] = P::out(q0, ep); psi[i1] = P::out(q1, ep);
+        lam[i0] = P::out(m0, el); lam[i1] = P::out(m1, el);
+      } else {
+        typename P::T q0 = P::in(p0), q1 = P::in(p1), m0 = P::in(l0), m1 = P::in(l1);
+        apply_dyn<P>(op.cls, m, q0, q1);
+        apply_dyn<P>(op.cls, m, m0, m1);
+        psi[i0] = P::out(q0); psi[i1] = P::out(q1);
+        lam[i0] = P::out(m0); lam[i1] = P::out(m1);
+      }
     }
   }
   if (gen != 0) {
@@ -550,12 +563,21 @@ int launch_adjoint_step_impl(dmv_state_s* psi, dmv_state_s* lam, const Op& op, i
   const bool ctrl = op.ctrl_kind != CTRL_NONE && op.ctrl >= 0;
   const int64_t pairs = psi->N >> (ctrl ? 2 : 1);
   const int grid = adjoint_grid(pairs);
-  if (psi->precision == DMV_C128)
-    k_adjoint_step<double><<<grid, kRedThreads, 0, psi->stream>>>(
+  const int64_t tok = prof_begin(DMV_KERNEL_ADJOINT, psi->stream, (double)(apply ? 4 : 2) * (double)psi->amp_bytes() *
+                                                                       (ctrl ? 0.5 : 1.0));
+  if (psi->precision == DMV_C64)
+    k_adjoint_step<PolF32><<<grid, kRedThreads, 0, psi->stream>>>(
+        static_cast<float2*>(psi->amps), static_cast<float2*>(lam->amps), pairs, op, apply, partial_slot);
+  else if (psi->arith == ARITH_INT64 && op.unitary)
+    k_adjoint_step<PolFX><<<grid, kRedThreads, 0, psi->stream>>>(
+        static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
+  else if (psi->arith == ARITH_FP32X2)
+    k_adjoint_step<PolDF><<<grid, kRedThreads, 0, psi->stream>>>(
         static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
   else
-    k_adjoint_step<float><<<grid, kRedThreads, 0, psi->stream>>>(
-        static_cast<float2*>(psi->amps), static_cast<float2*>(lam->amps), pairs, op, apply, partial_slot);
+    k_adjoint_step<PolF64><<<grid, kRedThreads, 0, psi->stream>>>(
+        static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
+  prof_end(tok, psi->stream);
   count_launch();
   DMV_CUDA_TRY(cudaGetLastError());
   return DMV_OK;
@@ -566,7 +588,7 @@ int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const doubl
   // Forward from |0...0> with the fused plan.
   DMV_TRY(launch_set_zero(s));
   Plan plan;
-  PlanOptions opt;
+  const PlanOptions opt = plan_options_for(s, DMV_FUSE_WINDOW);
   DMV_TRY(build_plan(gates, s->n, s->precision, opt, plan));
   DMV_TRY(launch_plan(s, plan));
   std::vector<double> ez((size_t)s->n);

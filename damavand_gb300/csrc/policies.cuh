@@ -10,11 +10,13 @@
 
 #include "complex_ops.cuh"
 #include "df.cuh"
+#include "fx.cuh"
 #include "internal.h"
 
 namespace dmv {
 
 struct PolF64 {  // complex128, IEEE FP64 multiply-adds
+  static constexpr bool kBlockScaled = false;
   using G = double2;
   using T = double2;
   using Mat = M2<double>;
@@ -27,6 +29,7 @@ struct PolF64 {  // complex128, IEEE FP64 multiply-adds
 };
 
 struct PolF32 {  // complex64, FP32 multiply-adds
+  static constexpr bool kBlockScaled = false;
   using G = float2;
   using T = float2;
   using Mat = M2<float>;
@@ -39,6 +42,7 @@ struct PolF32 {  // complex64, FP32 multiply-adds
 };
 
 struct PolDF {  // complex128 storage, FP32-pair arithmetic (df.cuh)
+  static constexpr bool kBlockScaled = false;
   using G = double2;
   using T = float4;
   using Mat = DFMat;
@@ -64,6 +68,186 @@ struct PolDF {  // complex128 storage, FP32-pair arithmetic (df.cuh)
   __device__ static T in(const G& g) { return df_from_double2(g); }
   __device__ static G out(const T& t) { return df_to_double2(t); }
 };
+
+// complex128 storage, int64 block fixed-point arithmetic on the integer pipe
+// (fx.cuh). Conversions need the block's exponent, so tiles are staged by
+// tile_load_fx / tile_store_fx and pairs by pair_in / pair_out.
+struct PolFX {
+  static constexpr bool kBlockScaled = true;
+  using G = double2;
+  using T = longlong2;
+  using Mat = FXMat;
+  static Mat mat(const Op& op) {
+    Mat m;
+    for (int i = 0; i < 8; ++i) {
+      m.h[i] = op.fh[i];
+      m.l[i] = op.fl[i];
+    }
+    return m;
+  }
+  __device__ static Mat dmat(const Op& op) {
+    Mat m;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      m.h[i] = op.fh[i];
+      m.l[i] = op.fl[i];
+    }
+    return m;
+  }
+  template <int CLS>
+  __device__ static void apply(const Mat& m, T& a0, T& a1) { fx_apply_pair<CLS>(m, a0, a1); }
+  // A pair as its own block: 4 components, 2-norm at most 2x the largest.
+  __device__ static int pair_exponent(const G& g0, const G& g1) {
+    return max(max(fx_exponent(g0.x), fx_exponent(g0.y)), max(fx_exponent(g1.x), fx_exponent(g1.y)));
+  }
+  __device__ static T in(const G& g, int e) { return make_longlong2(fx_from_double(g.x, e), fx_from_double(g.y, e)); }
+  __device__ static G out(const T& t, int e) { return make_double2(fx_to_double(t.x, e), fx_to_double(t.y, e)); }
+};
+
+// (a0, a1) <- M (a0, a1) with the op class chosen at run time.
+template <typename P>
+__device__ __forceinline__ void apply_dyn(int cls, const typename P::Mat& m, typename P::T& a0, typename P::T& a1) {
+  switch (cls) {
+    case OP_SWAP: P::template apply<OP_SWAP>(m, a0, a1); break;
+    case OP_DIAG: P::template apply<OP_DIAG>(m, a0, a1); break;
+    case OP_ANTI: P::template apply<OP_ANTI>(m, a0, a1); break;
+    case OP_REAL: P::template apply<OP_REAL>(m, a0, a1); break;
+    default: P::template apply<OP_GENERAL>(m, a0, a1); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tile staging. Both tile kernels run 512 threads, so local index l of a tile
+// splits as l = tid + 512*u: the low 9 bits come from the thread, the rest
+// from the slot u. With `low` <= 9 always-local low qubits, the HBM offset of
+// element l is (tid's part) | (u's part), both fixed for the whole pass:
+// tid's part is computed once per thread, u's parts once per CTA into shared
+// memory. Each thread then issues up to 8 loads before it writes any of them
+// to shared memory, so a CTA keeps 8 x 512 x 16 bytes in flight.
+// ---------------------------------------------------------------------------
+constexpr int kTileThreads = 512;
+constexpr int kTileThreadBits = 9;
+constexpr int kMaxSlots = 16;  // tiles of up to 2^13 amplitudes
+
+// Offsets of a tile's elements relative to the tile base. `high` are the
+// global positions of the nh high local qubits (ascending).
+template <typename HighArray>
+__device__ __forceinline__ int64_t tile_thread_offset(int low, int nh, const HighArray& high) {
+  const uint32_t tid = threadIdx.x;
+  int64_t off = (int64_t)(tid & ((1u << low) - 1u));
+  const int from_tid = min(nh, kTileThreadBits - low);
+  for (int i = 0; i < from_tid; ++i) off |= (int64_t)((tid >> (low + i)) & 1u) << high[i];
+  return off;
+}
+
+template <typename HighArray>
+__device__ __forceinline__ void tile_slot_offsets(int low, int nh, const HighArray& high, int slots, int64_t* s_slot) {
+  const int from_tid = min(nh, kTileThreadBits - low);
+  if ((int)threadIdx.x < slots) {
+    const uint32_t u = threadIdx.x;
+    int64_t off = 0;
+    for (int i = from_tid; i < nh; ++i) off |= (int64_t)((u >> (i - from_tid)) & 1u) << high[i];
+    s_slot[threadIdx.x] = off;
+  }
+}
+
+// HBM -> shared memory (converted to the working type). `cg` selects L2-only loads.
+template <typename P, bool CG>
+__device__ __forceinline__ void tile_load(typename P::T* tile, const typename P::G* a, int64_t base, int T,
+                                          int64_t t_off, const int64_t* s_slot) {
+  using G = typename P::G;
+  // Loads in flight per thread: 4 x 16 B or 8 x 8 B, i.e. 64 KB per SM at
+  // two CTAs, above what HBM latency needs, without spilling registers.
+  constexpr int B = sizeof(G) >= 16 ? 4 : 8;
+  const int slots = (T + kTileThreads - 1) >> kTileThreadBits;
+  for (int u0 = 0; u0 < slots; u0 += B) {
+    G v[B];
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int l = (int)threadIdx.x + ((u0 + j) << kTileThreadBits);
+      if (u0 + j < slots && l < T) {
+        const G* p = a + (base | t_off | s_slot[u0 + j]);
+        if constexpr (CG) v[j] = __ldcg(p);
+        else v[j] = *p;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int l = (int)threadIdx.x + ((u0 + j) << kTileThreadBits);
+      if (u0 + j < slots && l < T) tile[l] = P::in(v[j]);
+    }
+  }
+}
+
+template <typename P>
+__device__ __forceinline__ void tile_store(const typename P::T* tile, typename P::G* a, int64_t base, int T,
+                                           int64_t t_off, const int64_t* s_slot) {
+  const int slots = (T + kTileThreads - 1) >> kTileThreadBits;
+  for (int u = 0; u < slots; ++u) {
+    const int l = (int)threadIdx.x + (u << kTileThreadBits);
+    if (l < T) a[base | t_off | s_slot[u]] = P::out(tile[l]);
+  }
+}
+
+// Block-scaled staging (PolFX): the raw FP64 bits go to shared memory while
+// each thread tracks its largest exponent; a block-wide maximum (s_red: 16
+// ints) fixes the tile's exponent; each thread then converts the elements it
+// loaded, in place. Returns the tile exponent. The caller synchronises before
+// the ops, as after tile_load. Tiles of up to 4096 amplitudes keep every
+// fixed-point component below 2^60.5 (fx.cuh).
+template <bool CG>
+__device__ __forceinline__ int tile_load_fx(longlong2* tile, const double2* a, int64_t base, int T, int64_t t_off,
+                                            const int64_t* s_slot, int* s_red) {
+  const int slots = (T + kTileThreads - 1) >> kTileThreadBits;
+  unsigned emax = 0;
+  for (int u0 = 0; u0 < slots; u0 += 4) {
+    double2 v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int l = (int)threadIdx.x + ((u0 + j) << kTileThreadBits);
+      if (u0 + j < slots && l < T) {
+        const double2* p = a + (base | t_off | s_slot[u0 + j]);
+        if constexpr (CG) v[j] = __ldcg(p);
+        else v[j] = *p;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int l = (int)threadIdx.x + ((u0 + j) << kTileThreadBits);
+      if (u0 + j < slots && l < T) {
+        tile[l] = make_longlong2(__double_as_longlong(v[j].x), __double_as_longlong(v[j].y));
+        emax = max(emax, (unsigned)max(fx_exponent(v[j].x), fx_exponent(v[j].y)));
+      }
+    }
+  }
+  emax = __reduce_max_sync(0xffffffffu, emax);
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = (int)emax;
+  __syncthreads();
+  int e = 0;
+#pragma unroll
+  for (int w = 0; w < kTileThreads / 32; ++w) e = max(e, s_red[w]);
+  for (int u = 0; u < slots; ++u) {
+    const int l = (int)threadIdx.x + (u << kTileThreadBits);
+    if (l < T) {
+      const longlong2 r = tile[l];
+      tile[l] = make_longlong2(fx_from_double(__longlong_as_double(r.x), e),
+                               fx_from_double(__longlong_as_double(r.y), e));
+    }
+  }
+  return e;
+}
+
+__device__ __forceinline__ void tile_store_fx(const longlong2* tile, double2* a, int64_t base, int T, int64_t t_off,
+                                              const int64_t* s_slot, int e) {
+  const int slots = (T + kTileThreads - 1) >> kTileThreadBits;
+  for (int u = 0; u < slots; ++u) {
+    const int l = (int)threadIdx.x + (u << kTileThreadBits);
+    if (l < T) {
+      const longlong2 x = tile[l];
+      a[base | t_off | s_slot[u]] = make_double2(fx_to_double(x.x, e), fx_to_double(x.y, e));
+    }
+  }
+}
 
 // One op over a tile of T amplitudes in shared memory, all threads of the CTA.
 template <typename P, int CLS>

@@ -23,7 +23,10 @@ def _rotation_layers(n: int, layers: int, rng: np.random.Generator, ring: bool):
         for q in range(n):
             for kind in (RX, RY, RZ):
                 gates.append((kind, q, -1, False, float(rng.uniform(0.0, 2.0 * math.pi))))
-        pairs = [(i, (i + 1) % n) for i in range(n)] if ring else [(i, i + 1) for i in range(n - 1)]
+        if ring:
+            pairs = [(i, (i + 1) % n) for i in range(n)] if n > 1 else []  # one qubit: no ring edge
+        else:
+            pairs = [(i, i + 1) for i in range(n - 1)]
         for c, t in pairs:
             gates.append((CNOT, t, c, False, 0.0))
     return gates

@@ -52,12 +52,17 @@ enum {
 enum { DMV_C128 = 0, DMV_C64 = 1 };
 
 /* Arithmetic of complex128 gate application (complex64 always computes in FP32).
+ * The amplitudes stay IEEE complex128 in device memory in every mode.
  * DMV_ARITH_FP64: IEEE FP64 multiply-adds (default).
  * DMV_ARITH_FP32X2: the FP64 amplitudes are split into FP32 pairs (about 48
  *   significant bits) inside each kernel and combined with error-free
  *   transformations, then stored back as FP64; GB300 runs FP32 ~71x faster
- *   than FP64. Measured error on deep circuits ~1e-13 normwise. */
-enum { DMV_ARITH_FP64 = 0, DMV_ARITH_FP32X2 = 1 };
+ *   than FP64. Measured error on deep circuits ~1e-13 normwise.
+ * DMV_ARITH_INT64: each tile (or pair) is converted to int64 fixed point with
+ *   one shared exponent (54 fraction bits for its largest components) and
+ *   multiplied exactly in 31-bit limbs on the integer pipe, with one rounding
+ *   per output. Passes holding a non-unitary matrix fall back to FP64. */
+enum { DMV_ARITH_FP64 = 0, DMV_ARITH_FP32X2 = 1, DMV_ARITH_INT64 = 2 };
 
 /* Gate kinds (numbering shared with the oracle). DMV_GATE_MATRIX takes an
  * explicit 2x2 matrix; every kind may carry a control qubit. */
@@ -160,6 +165,12 @@ int dmv_apply_matrix(dmv_state_t s, const double m_re[4], const double m_im[4],
 int dmv_apply_gates(dmv_state_t s, const dmv_gate_t* gates, int64_t num_gates, int32_t fusion);
 /* Number of HBM passes the last dmv_apply_gates call used (plan statistics). */
 int dmv_last_plan_stats(int64_t* num_passes, int64_t* num_fused_ops, int64_t* bytes_moved);
+/* Plans a gate list without touching a GPU (host only): the number of HBM
+ * passes, of window passes, of ops after merging, and the largest number of
+ * local qubits of a window. tile_bits 0 picks the default for the precision. */
+int dmv_plan_describe(int32_t num_qubits, int32_t precision, const dmv_gate_t* gates, int64_t num_gates,
+                      int32_t fusion, int32_t tile_bits, int64_t* num_passes, int64_t* num_window_passes,
+                      int64_t* num_ops, int32_t* max_local_qubits);
 
 /* ------------------------------------------------------------------------ */
 /* Measurement (synchronous: results are on the host when these return)      */
