@@ -43,7 +43,10 @@ sys.path.insert(0, REPO)
 METRIC = "30-qubit gate applies/s + HBM GB/s; adjoint vs param-shift grads/s at 1e-10"
 UNIT = "gate-applies/s"
 DTYPES = {"fp64": "f64 (complex128 storage and FP64 arithmetic)",
-          "fp32x2": "f32x2 (complex128 storage, FP32-pair arithmetic, ~48-bit)"}
+          "fp32x2": "f32x2 (complex128 storage, FP32-pair arithmetic, ~48-bit)",
+          "int64": "int64 (complex128 storage, block fixed point: 54-bit fraction per tile, exact products)"}
+# Integer multiply-add (IMAD) throughput of a GB300 measured with an independent-chain kernel.
+INT_MAD_PEAK_T = 18.85
 # FP64 multiply-add throughput of a GB300 measured with an independent-FMA-chain kernel
 # (0.504 T FMA/s = 1.0 TFLOP/s); complex128 arithmetic is bounded by it.
 FP64_FMA_PEAK_T = 0.504
@@ -407,6 +410,10 @@ def rooflines(fam, n, arith):
     if arith == "fp64":
         ra = {"bound": "fp64", "achieved": rate, "peak": FP64_FMA_PEAK_T, "unit": "T FMA/s",
               "frac": rate / FP64_FMA_PEAK_T, "peak_source": "measured (FP64 FMA chain kernel on this pool's GB300)"}
+    elif arith == "int64":
+        ra = {"bound": "int-mad", "achieved": rate, "peak": INT_MAD_PEAK_T, "unit": "T IMAD/s",
+              "frac": rate / INT_MAD_PEAK_T,
+              "peak_source": "measured (32-bit IMAD chain kernel on this pool's GB300); counts IMAD.WIDE limb products"}
     else:
         ra = {"bound": "fp32", "achieved": rate, "peak": FP32_FMA_PEAK_T, "unit": "T op/s",
               "frac": rate / FP32_FMA_PEAK_T, "peak_source": "measured (FP32 FMA chain kernel on this pool's GB300)"}
@@ -501,26 +508,35 @@ def run_ours(args, world, rank, local):
                       "norm": float(c.norm()), "first_samples": [int(x) for x in samples[:4]],
                       "mean_abs_expect_z": float(np.mean(np.abs(ez)))}
 
-    # ---- the other complex128 arithmetic, same workload and protocol, checked against this one
+    # ---- the other complex128 arithmetics, same workload and protocol, each checked against FP64
     if not args.no_alt:
         import torch
-        alt = "fp32x2" if args.arith == "fp64" else "fp64"
-        c2 = Circuit(n, "gpu", fusion=not args.no_fusion, arithmetic=alt)
-        add_to_circuit(c2, gates)
-        ms2, fam2, launches2, clocks2, _ = timed_forward(c2, args, world, local)
-        rl2, ra2, gbs2 = rooflines(fam2, n, alt)
-        ta, tb = c2.state().torch(), c.state().torch()  # both hold one forward from |0...0>
-        ref, other = (tb, ta) if args.arith == "fp64" else (ta, tb)
-        err = normwise_err(other, ref)
-        del ta, tb, ref, other
-        out["alt_arithmetic"] = {
-            "arithmetic": alt, "dtype": DTYPES[alt], "value": world * G / (ms2 / 1e3), "unit": UNIT,
-            "ms_per_step": ms2, "roofline": rl2, "roofline_arith": ra2, "hbm_gbs_pass_bytes": gbs2,
-            "gpu_launches": int(launches2), "clocks": clocks2,
-            "parity": {"against": "the FP64-arithmetic forward of this run", "normwise_max_err": err,
-                       "tolerance": 1e-12, "ok": err <= 1e-12}}
-        del c2
-        torch.cuda.empty_cache()
+        alts = [a for a in ("fp64", "fp32x2", "int64") if a != args.arith]
+        out["alt_arithmetic"] = []
+        for alt in alts:
+            c2 = Circuit(n, "gpu", fusion=not args.no_fusion, arithmetic=alt)
+            add_to_circuit(c2, gates)
+            ms2, fam2, launches2, clocks2, _ = timed_forward(c2, args, world, local)
+            rl2, ra2, gbs2 = rooflines(fam2, n, alt)
+            ta, tb = c2.state().torch(), c.state().torch()  # both hold one forward from |0...0>
+            if args.arith == "fp64":
+                ref, other = tb, ta
+            elif alt == "fp64":
+                ref, other = ta, tb
+            else:
+                ref, other = None, None
+            err = normwise_err(other, ref) if ref is not None else None
+            del ta, tb, ref, other
+            entry = {
+                "arithmetic": alt, "dtype": DTYPES[alt], "value": world * G / (ms2 / 1e3), "unit": UNIT,
+                "ms_per_step": ms2, "roofline": rl2, "roofline_arith": ra2, "hbm_gbs_pass_bytes": gbs2,
+                "gpu_launches": int(launches2), "clocks": clocks2}
+            if err is not None:
+                entry["parity"] = {"against": "the FP64-arithmetic forward of this run", "normwise_max_err": err,
+                                   "tolerance": 1e-12, "ok": err <= 1e-12}
+            out["alt_arithmetic"].append(entry)
+            del c2
+            torch.cuda.empty_cache()
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = adjoint_section(args)
     if rank == 0 and not args.no_batch:
@@ -542,9 +558,10 @@ def main():
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--no-fusion", action="store_true")
     ap.add_argument("--no-alt", action="store_true",
-                    help="skip the second complex128 arithmetic (timed and checked against the first)")
-    ap.add_argument("--arith", choices=["fp64", "fp32x2"], default="fp64",
-                    help="complex128 arithmetic: IEEE FP64, or FP32 pairs (error-free transformations)")
+                    help="skip the other complex128 arithmetics (timed and checked against FP64)")
+    ap.add_argument("--arith", choices=["fp64", "fp32x2", "int64"], default="fp64",
+                    help="complex128 arithmetic: IEEE FP64, FP32 pairs (error-free transformations), "
+                         "or int64 block fixed point")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--workload", choices=["default", "large"], default="default",
