@@ -390,7 +390,7 @@ def timed_forward(c, args, world, local):
     return step_ms, read_families(lib, check), launches, clocks.summary(), step
 
 
-def rooflines(fam, n, arith):
+def rooflines(fam, n, arith, prec="c128"):
     dom = max(fam, key=lambda k: fam[k]["ms"])
     d = fam[dom]
     peak, peak_kind = load_peaks()
@@ -399,8 +399,8 @@ def rooflines(fam, n, arith):
     achieved = per_launch_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
     # DRAM bytes per launch from one ncu capture (profiles/*_full.md), scaled by state size.
     traffic = None
-    if (dom, "c128") in NCU_TRAFFIC_PER_AMPLITUDE:
-        traffic = NCU_TRAFFIC_PER_AMPLITUDE[(dom, "c128")] * (1 << n)
+    if (dom, prec) in NCU_TRAFFIC_PER_AMPLITUDE:
+        traffic = NCU_TRAFFIC_PER_AMPLITUDE[(dom, prec)] * (1 << n)
     roofline = {"bound": "hbm", "kernel": f"k_apply_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_launch_s * 1e3}
@@ -537,6 +537,21 @@ def run_ours(args, world, rank, local):
             out["alt_arithmetic"].append(entry)
             del c2
             torch.cuda.empty_cache()
+        # complex64 storage and FP32 arithmetic, same workload and protocol (the
+        # TMA window kernel's register-phase variant); error against this run's
+        # complex128 state.
+        c3 = Circuit(n, "gpu", fusion=not args.no_fusion, precision="complex64")
+        add_to_circuit(c3, gates)
+        ms3, fam3, launches3, clocks3, _ = timed_forward(c3, args, world, local)
+        rl3, ra3, gbs3 = rooflines(fam3, n, "fp32", prec="c64")
+        err = normwise_err(c3.state().torch(), c.state().torch())
+        out["complex64"] = {
+            "dtype": "c64 (complex64 storage, FP32 arithmetic)", "value": world * G / (ms3 / 1e3), "unit": UNIT,
+            "ms_per_step": ms3, "roofline": rl3, "roofline_arith": ra3, "hbm_gbs_pass_bytes": gbs3,
+            "gpu_launches": int(launches3), "clocks": clocks3,
+            "error": {"against": f"the {args.arith} complex128 forward of this run", "normwise_max_err": err}}
+        del c3
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_adjoint:
         out["adjoint"] = adjoint_section(args)
     if rank == 0 and not args.no_batch:

@@ -95,6 +95,7 @@ SIGNATURES = {
     "dmv_batch_stats": (ctypes.c_int, [_vp, _i64p, _i64p, _i64p, _i32p, _dp]),
     "dmv_batch_debug_wait_limit": (ctypes.c_int, [_vp, _i64, _i32]),
     "dmv_debug_fail_allocations": (ctypes.c_int, [_i32]),
+    "dmv_debug_tma_wait_limit": (ctypes.c_int, [_i64]),
     "dmv_circuit_create": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, _vpp]),
     "dmv_circuit_destroy": (ctypes.c_int, [_vp]),
     "dmv_circuit_add_gate": (ctypes.c_int, [_vp, _i32, _i32, _i32, _f64, _i32]),

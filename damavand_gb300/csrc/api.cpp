@@ -303,6 +303,11 @@ extern "C" int dmv_debug_fail_allocations(int32_t count) {
   return DMV_OK;
 }
 
+extern "C" int dmv_debug_tma_wait_limit(int64_t polls) {
+  dmv::set_tma_wait_limit(polls);
+  return DMV_OK;
+}
+
 extern "C" int dmv_set_device(int32_t device) {
   clear_error();
   DMV_CUDA_TRY(cudaSetDevice(device));
@@ -409,6 +414,7 @@ extern "C" int dmv_state_destroy(dmv_state_t s) {
   if (s->amps) cudaFree(s->amps);
   s->amps = nullptr;
   s->ops_dev.release();
+  s->phase_ops_dev.release();
   s->reduce_dev.release();
   s->chunk_dev.release();
   if (s->pinned) cudaFreeHost(s->pinned);
@@ -447,6 +453,7 @@ extern "C" int dmv_state_synchronize(dmv_state_t s) {
   clear_error();
   DMV_TRY(check_state(s));
   DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  DMV_TRY(dmv::check_window_status());
   return DMV_OK;
 }
 
@@ -540,6 +547,16 @@ extern "C" int dmv_apply_matrix(dmv_state_t s, const double m_re[4], const doubl
   return apply_gate_list(s, gates, DMV_FUSE_NONE);
 }
 
+namespace {
+// Launch statistics of the last gate list applied on this thread (dmv_last_plan_stats).
+thread_local int64_t g_stat_passes = 0, g_stat_ops = 0, g_stat_bytes = 0;
+void record_stats(dmv_state_s* s) {
+  g_stat_passes = s->last_passes;
+  g_stat_ops = s->last_ops;
+  g_stat_bytes = s->last_bytes;
+}
+}  // namespace
+
 extern "C" int dmv_apply_gates(dmv_state_t s, const dmv_gate_t* gates, int64_t num_gates, int32_t fusion) {
   clear_error();
   DMV_TRY(check_state(s));
@@ -547,7 +564,9 @@ extern "C" int dmv_apply_gates(dmv_state_t s, const dmv_gate_t* gates, int64_t n
     return set_error(DMV_ERR_INVALID, "unknown fusion mode %d", fusion);
   std::vector<Gate> parsed;
   DMV_TRY(parse_gates(gates, num_gates, s->n, parsed));
-  return apply_gate_list(s, parsed, fusion);
+  DMV_TRY(apply_gate_list(s, parsed, fusion));
+  record_stats(s);
+  return DMV_OK;
 }
 
 extern "C" int dmv_plan_describe(int32_t num_qubits, int32_t precision, const dmv_gate_t* gates, int64_t num_gates,
@@ -582,24 +601,12 @@ extern "C" int dmv_plan_describe(int32_t num_qubits, int32_t precision, const dm
   return DMV_OK;
 }
 
-namespace {
-thread_local int64_t g_stat_passes = 0, g_stat_ops = 0, g_stat_bytes = 0;
-}
-
 extern "C" int dmv_last_plan_stats(int64_t* num_passes, int64_t* num_fused_ops, int64_t* bytes_moved) {
   if (num_passes) *num_passes = g_stat_passes;
   if (num_fused_ops) *num_fused_ops = g_stat_ops;
   if (bytes_moved) *bytes_moved = g_stat_bytes;
   return DMV_OK;
 }
-
-namespace {
-void record_stats(dmv_state_s* s) {
-  g_stat_passes = s->last_passes;
-  g_stat_ops = s->last_ops;
-  g_stat_bytes = s->last_bytes;
-}
-}  // namespace
 
 // ===========================================================================
 // Measurement

@@ -314,4 +314,66 @@ int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
   return DMV_OK;
 }
 
+int64_t assign_phases(Op* ops, int64_t count, int32_t tile_bits, int32_t rb) {
+  // Phases are built by list scheduling: each phase sweeps the remaining ops
+  // in order (up to kLookahead of them) and takes every op whose target is,
+  // or can still become, one of the phase's rb register bits and none of
+  // whose tile bits is used by an op the sweep left behind. Ops that share
+  // no tile bit commute, so the order within the pass may change; ops that
+  // share one keep their order.
+  constexpr int64_t kLookahead = 256;
+  const std::vector<Op> in(ops, ops + count);
+  std::vector<char> done((size_t)count, 0);
+  int64_t out = 0, first = 0, phases = 0;
+  while (out < count) {
+    while (done[(size_t)first]) ++first;
+    int32_t reg[kMaxRegBits] = {0, 0, 0, 0};
+    int32_t nr = 0;
+    uint32_t rmask = 0, blocked = 0;
+    const int64_t begin = out;
+    int64_t seen = 0;
+    for (int64_t i = first; i < count && seen < kLookahead; ++i) {
+      if (done[(size_t)i]) continue;
+      ++seen;
+      const Op& op = in[(size_t)i];
+      uint32_t qs = 1u << op.target;
+      if (op.ctrl_kind == CTRL_LOCAL) qs |= 1u << op.ctrl;
+      if (qs & blocked) {
+        blocked |= qs;
+        continue;
+      }
+      if (!((rmask >> op.target) & 1u)) {
+        if (nr == rb) {
+          blocked |= qs;
+          continue;
+        }
+        reg[nr++] = op.target;
+        rmask |= 1u << op.target;
+      }
+      ops[out++] = op;
+      done[(size_t)i] = 1;
+    }
+    for (int32_t pos = 0; nr < rb && pos < tile_bits; ++pos)
+      if (!((rmask >> pos) & 1u)) {
+        reg[nr++] = pos;
+        rmask |= 1u << pos;
+      }
+    for (int64_t j = begin; j < out; ++j) {
+      Op& op = ops[j];
+      uint32_t v = 0;
+      if (j == begin) {
+        v |= kPhaseStart;
+        for (int32_t b = 0; b < rb; ++b) v |= (uint32_t)reg[b] << (4 * b);
+      }
+      for (int32_t b = 0; b < rb; ++b) {
+        if (reg[b] == op.target) v |= (uint32_t)b << kPhaseTargetShift;
+        if (op.ctrl_kind == CTRL_LOCAL && reg[b] == op.ctrl) v |= (uint32_t)(b + 1) << kPhaseCtrlShift;
+      }
+      op.phase = (int32_t)v;
+    }
+    ++phases;
+  }
+  return phases;
+}
+
 }  // namespace dmv

@@ -83,9 +83,43 @@ struct alignas(16) Op {
   int32_t param;      // index of the gradient slot (adjoint) or -1
   int32_t generator;  // 0 none, 1 X, 2 Y, 3 Z: generator of a rotation (adjoint)
   int32_t unitary;    // 1 when m is unitary to 1e-12 (block fixed point relies on it)
-  int32_t pad;
+  int32_t phase;      // register phase of a fused op (kPhase* below), 0 elsewhere
 };
 static_assert(sizeof(Op) == 224, "Op layout");
+
+// Register phases of a fused pass run by the TMA window kernel: each thread
+// keeps 2^rb amplitudes of the tile in registers, the ones that differ in rb
+// "register bits" of the tile index, and applies every op whose target is a
+// register bit without touching shared memory. An op that starts a phase
+// carries the phase's register bits; the tile goes through shared memory only
+// between phases.
+constexpr uint32_t kPhaseStart = 0x80000000u;  // this op starts a phase
+// bits 0..15: the phase's register bits, 4 bits each (valid on a phase start)
+// bits 16..17: index of the op's target among the register bits
+// bits 20..22: 1 + index of the op's local control among them, 0 if not one
+constexpr int kPhaseTargetShift = 16;
+constexpr int kPhaseCtrlShift = 20;
+constexpr int kMaxRegBits = 4;
+
+// An op as the register-phase kernel reads it from its shared-memory op
+// table (complex64 passes): the FP32 matrix and the fields the loop tests.
+struct alignas(16) PhaseOp {
+  float m[8];         // op.mh: the matrix rounded to FP32
+  uint32_t phase;     // op.phase
+  int32_t ctrl;
+  int32_t ctrl_kind;
+  int32_t cls;
+};
+static_assert(sizeof(PhaseOp) == 48, "PhaseOp layout");
+// Ops one launch of the register-phase kernel holds in shared memory; a
+// longer pass runs as several launches over the same qubits.
+constexpr int64_t kMaxPhaseOps = 128;
+
+// Orders one fused pass's ops (tile-local targets) into register phases and
+// marks them: each phase holds ops whose targets span at most rb tile bits
+// (padded with unused tile bits); ops move across others only where they
+// share no tile bit. Returns the number of phases.
+int64_t assign_phases(Op* ops, int64_t count, int32_t tile_bits, int32_t rb);
 
 // Fills op.mh / op.ml (FP32 pair: hi = nearest float, lo = nearest float of
 // the rest), op.fh / op.fl (Q.54 limbs) and op.unitary from op.m.
@@ -175,6 +209,10 @@ struct dmv_state_s {
   dmv::DeviceBuffer reduce_dev;  // reduction partials
   dmv::DeviceBuffer chunk_dev;   // per-chunk probability sums (sampling)
   std::vector<dmv::Op> ops_host_pinned;  // (regular host memory; copied async from a pinned staging)
+  std::vector<dmv::Op> ops_staging;      // plan ops with register phases marked, as uploaded
+  std::vector<dmv::Pass> pass_staging;   // the launches of the last plan (long phase passes split)
+  std::vector<dmv::PhaseOp> phase_ops;   // compact ops of the register-phase launches
+  dmv::DeviceBuffer phase_ops_dev;
   void* pinned = nullptr;        // pinned host staging
   size_t pinned_bytes = 0;
   int64_t last_passes = 0, last_ops = 0, last_bytes = 0;
@@ -185,13 +223,13 @@ struct dmv_state_s {
 namespace dmv {
 int ensure_pinned(dmv_state_s* s, size_t bytes);
 
-// Planner settings for a state: complex64 tiles hold 2^13 amplitudes (64 KB of
-// shared memory, like a 2^12 complex128 tile), so each HBM pass covers one
-// more qubit.
+// Planner settings for a state: tiles of 2^12 amplitudes (the TMA window
+// kernel's register phases hold 8 per thread of 512).
 inline PlanOptions plan_options_for(const dmv_state_s* s, int32_t fusion) {
+  (void)s;
   PlanOptions opt;
   opt.fusion = fusion;
-  opt.tile_bits = s->precision == DMV_C64 ? 13 : 12;
+  opt.tile_bits = 12;
   return opt;
 }
 
@@ -210,6 +248,11 @@ int launch_adjoint_step(dmv_state_s* psi, dmv_state_s* lam, const Op& op, double
 int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const double* weights,
                      double* loss, double* grads);
 int upload_ops(dmv_state_s* s, const Op* ops, int64_t count);
+// DMV_ERR_TIMEOUT (and clears the flag) when a TMA window pass gave up
+// waiting for a tile load since the last check; synchronises the device.
+int check_window_status();
+// Polls before a TMA tile-load wait gives up; negative restores the default.
+void set_tma_wait_limit(int64_t polls);
 
 // Chunk-mass / Pauli-Z reduction into caller-provided device buffers:
 // `mass` holds num_chunks doubles, `partial` partial_elems, `sums` n+1

@@ -34,7 +34,15 @@ struct PolF32 {  // complex64, FP32 multiply-adds
   using T = float2;
   using Mat = M2<float>;
   static Mat mat(const Op& op) { return to_m2<float>(op.m); }
-  __device__ static Mat dmat(const Op& op) { return to_m2<float>(op.m); }
+  // op.mh holds the entries rounded to nearest FP32, the same values as
+  // to_m2<float>(op.m), without device FP64->FP32 conversions (those run on
+  // the FP64 pipe).
+  __device__ static Mat dmat(const Op& op) {
+    Mat m;
+    m.r00 = op.mh[0]; m.i00 = op.mh[1]; m.r01 = op.mh[2]; m.i01 = op.mh[3];
+    m.r10 = op.mh[4]; m.i10 = op.mh[5]; m.r11 = op.mh[6]; m.i11 = op.mh[7];
+    return m;
+  }
   template <int CLS>
   __device__ static void apply(const Mat& m, T& a0, T& a1) { apply_pair<float, CLS>(m, a0, a1); }
   __device__ static T in(const G& g) { return g; }

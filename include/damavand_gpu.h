@@ -251,6 +251,11 @@ int dmv_batch_debug_wait_limit(dmv_batch_t b, int64_t spin_limit, int32_t poison
 /* Test hook: the next `count` device allocations of the library fail (as if
  * out of memory). */
 int dmv_debug_fail_allocations(int32_t count);
+/* Test hook: the number of polls after which a TMA window pass stops waiting
+ * for a tile load (negative: the default). The pass then drains its copies,
+ * leaves the state undefined and the next dmv_state_synchronize returns
+ * DMV_ERR_TIMEOUT. No reference counterpart. */
+int dmv_debug_tma_wait_limit(int64_t polls);
 
 /* ------------------------------------------------------------------------ */
 /* Circuit front-end (the reference's pyo3 Circuit, src/qubit_backend/circuit.rs:78-770) */

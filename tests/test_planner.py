@@ -42,12 +42,14 @@ def test_config2_plan_shape(built_lib):
     assert rc == 0 and passes_none == ops_none == count(gates) == 2410
 
 
-def test_complex64_windows_hold_13_qubits(built_lib):
+def test_complex64_windows_match_complex128(built_lib):
+    """Both precisions plan 12-qubit tiles (the TMA kernel's register phases hold 8
+    amplitudes per thread of 512), so their plans coincide."""
     from damavand_gb300.workloads import ladder_circuit
     rc, passes, _, _, max_local = _describe(built_lib.lib, 30, ladder_circuit(30, 20, seed=1), precision=1)
-    assert rc == 0 and max_local == 13
+    assert rc == 0 and max_local == 12
     rc, passes128, _, _, _ = _describe(built_lib.lib, 30, ladder_circuit(30, 20, seed=1), precision=0)
-    assert passes <= passes128
+    assert passes == passes128
 
 
 @pytest.mark.parametrize("n", [1, 2, 5, 12])
