@@ -52,8 +52,13 @@ INT_MAD_PEAK_T = 18.85
 FP64_FMA_PEAK_T = 0.504
 FP32_FMA_PEAK_T = 35.9
 # dram__bytes_read.sum + dram__bytes_write.sum per launch divided by the amplitudes of
-# the captured case (profiles/k_apply_window_c128_24q_full.md: 493.7 MB at 2^24).
-NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 493.698304e6 / (1 << 24)}
+# the captured case (profiles/k_window_tma_fp64_24q_full.md: 479.9 MB at 2^24;
+# profiles/k_window_phases_c64_26q_full.md: 1012.3 MB at 2^26).
+NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 479.873280e6 / (1 << 24),
+                             ("window", "c64"): 1012.291328e6 / (1 << 26)}
+# The kernel that runs a fused window pass, by arithmetic and precision.
+WINDOW_KERNEL = {("fp64", "c128"): "k_window_tma<PolF64>", ("fp32x2", "c128"): "k_apply_window<PolDF>",
+                 ("int64", "c128"): "k_apply_window<PolFX>", ("fp32", "c64"): "k_window_phases<PolF32>"}
 
 
 def load_peaks():
@@ -401,7 +406,8 @@ def rooflines(fam, n, arith, prec="c128"):
     traffic = None
     if (dom, prec) in NCU_TRAFFIC_PER_AMPLITUDE:
         traffic = NCU_TRAFFIC_PER_AMPLITUDE[(dom, prec)] * (1 << n)
-    roofline = {"bound": "hbm", "kernel": f"k_apply_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    kernel = WINDOW_KERNEL.get((arith, prec), "window") if dom == "window" else f"k_apply_{dom}"
+    roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_launch_s * 1e3}
     # The same kernel against the arithmetic ceiling it meets on GB300: FP64

@@ -82,3 +82,21 @@ def test_host_side_validation_without_gpu(built_lib):
                                         u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1,
                                         s.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))) == 1
     assert lib.peer_access_allowed(0, 1) == 0
+
+
+def test_reference_import_name(built_lib):
+    """`from damavand import Circuit` (the reference's pyo3 module name) is this
+    library's Circuit, with the pyo3 method names."""
+    import damavand
+    from damavand.circuit import Circuit as C2
+
+    from damavand_gb300 import Circuit
+    assert damavand.Circuit is Circuit and C2 is Circuit
+    for name in ("add_hadamard_gate", "add_rotation_x_gate", "add_rotation_y_gate", "add_rotation_z_gate",
+                 "add_pauli_x_gate", "add_pauli_y_gate", "add_pauli_z_gate", "add_cnot_gate", "forward",
+                 "measure", "sample", "sample_local", "extract_expectation_values", "set_parameters",
+                 "reset", "reset_amplitudes", "retrieve_amplitudes_on_host", "get_real_part_state",
+                 "get_imaginary_part_state", "print_operations",
+                 "get_fidelity_between_two_states_with_parameters"):
+        assert callable(getattr(Circuit, name)), name
+    damavand.initialize_mpi()
