@@ -303,6 +303,13 @@ extern "C" int dmv_debug_fail_allocations(int32_t count) {
   return DMV_OK;
 }
 
+extern "C" int dmv_debug_tc_convert(int32_t mode) {
+  clear_error();
+  if (mode != 0 && mode != 1) return set_error(DMV_ERR_INVALID, "tensor-core conversion mode must be 0 or 1");
+  dmv::set_tc_convert_mode(mode);
+  return DMV_OK;
+}
+
 extern "C" int dmv_debug_tma_wait_limit(int64_t polls) {
   dmv::set_tma_wait_limit(polls);
   return DMV_OK;
@@ -443,7 +450,8 @@ extern "C" int dmv_state_set_zero(dmv_state_t s) {
 extern "C" int dmv_state_set_arithmetic(dmv_state_t s, int32_t arithmetic) {
   clear_error();
   DMV_TRY(check_state(s));
-  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2 && arithmetic != DMV_ARITH_INT64)
+  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2 && arithmetic != DMV_ARITH_INT64 &&
+      arithmetic != DMV_ARITH_TC)
     return set_error(DMV_ERR_INVALID, "unknown arithmetic %d", arithmetic);
   s->arith = arithmetic;
   return DMV_OK;
@@ -598,6 +606,15 @@ extern "C" int dmv_plan_describe(int32_t num_qubits, int32_t precision, const dm
   if (num_window_passes) *num_window_passes = windows;
   if (num_ops) *num_ops = (int64_t)plan.ops.size();
   if (max_local_qubits) *max_local_qubits = max_local;
+  return DMV_OK;
+}
+
+extern "C" int dmv_last_tc_stats(dmv_state_t s, int64_t* tc_passes, int64_t* blocks, int64_t* exchanges) {
+  clear_error();
+  DMV_TRY(check_state(s));
+  if (tc_passes) *tc_passes = s->last_tc_passes;
+  if (blocks) *blocks = s->last_tc_blocks;
+  if (exchanges) *exchanges = s->last_tc_swaps;
   return DMV_OK;
 }
 

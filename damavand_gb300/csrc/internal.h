@@ -129,7 +129,8 @@ void split_matrix(Op& op);
 enum Arith : int32_t {
   ARITH_FP64 = 0,    // IEEE FP64 multiply-adds
   ARITH_FP32X2 = 1,  // FP32-pair (double-float) error-free transformations
-  ARITH_INT64 = 2    // int64 block fixed point on the integer pipe
+  ARITH_INT64 = 2,   // int64 block fixed point on the integer pipe
+  ARITH_TC = 3       // int64 block fixed point, dense blocks as exact digit products on the tensor cores
 };
 
 // Host-side gate after parsing.
@@ -185,6 +186,44 @@ int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
                const PlanOptions& opt, Plan& plan);
 
 // ---------------------------------------------------------------------------
+// Tensor-core window passes (ARITH_TC, complex128 storage).
+//
+// The tile (2^12 amplitudes) is held as int64 block fixed point. A pass is
+// cut into stages: exchanges (X, CNOT: integer swaps in shared memory) and
+// dense blocks, the product of consecutive ops on at most 5 tile bits as one
+// 32 x 32 complex matrix. A block is applied to the tile viewed as 128
+// columns of 32 amplitudes: every integer is split into 7 balanced 8-bit
+// digits (FP16, exact), the matrix likewise, and the 34 digit products
+// whose weights 2^(-8s) have s = i + j <= 7 accumulate exactly in FP32 on the
+// tensor cores (tcgen05.mma), one TMEM accumulator per weight.
+// ---------------------------------------------------------------------------
+constexpr int kTcBlockBits = 5;                             // qubits of a dense block
+constexpr int kTcDigits = 7;                                // balanced 8-bit digits of a 56-bit integer
+constexpr int kTcURows = 64 * kTcDigits;                    // rows of a block's stacked digit matrix
+constexpr int64_t kTcUHalves = (int64_t)kTcURows * 64;      // FP16 elements per block (56 KB)
+enum TcStageKind : int32_t { TC_BLOCK = 0, TC_SWAP = 1 };
+
+struct TcStage {
+  int32_t kind;     // TcStageKind
+  int32_t bits[5];  // block: tile bits of block-row bits 0..4 (ascending); swap: [0] target, [1] local control or -1
+  int32_t gctrl;    // swap: control qubit outside the tile, or -1
+  int32_t u_index;  // block: index of its digit matrix in the plan's array
+  int32_t magic;    // block: 1 when every FP32 accumulator stays below 2^22 in magnitude
+  int32_t pad[3];
+};
+static_assert(sizeof(TcStage) == 48, "TcStage layout");
+
+// Cuts window pass `ps` of `plan` (a 2^12-amplitude tile) into stages,
+// appended to `stages`, and appends each block's digit matrix (kTcUHalves
+// FP16 bit patterns in the tensor cores' K-major layout) to `u`. Returns
+// false, appending nothing, when the pass holds an op the tensor-core kernel
+// does not take (a non-unitary op, or a non-exchange op controlled from
+// outside the tile).
+bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stages, std::vector<uint16_t>& u);
+// Test hook (dmv_debug_tc_convert): 1 forces the exact conversion in every block.
+void set_tc_convert_mode(int32_t mode);
+
+// ---------------------------------------------------------------------------
 // Device state
 // ---------------------------------------------------------------------------
 struct DeviceBuffer {
@@ -213,9 +252,13 @@ struct dmv_state_s {
   std::vector<dmv::Pass> pass_staging;   // the launches of the last plan (long phase passes split)
   std::vector<dmv::PhaseOp> phase_ops;   // compact ops of the register-phase launches
   dmv::DeviceBuffer phase_ops_dev;
+  std::vector<dmv::TcStage> tc_stages;  // tensor-core passes of the last plan
+  std::vector<uint16_t> tc_u;
+  dmv::DeviceBuffer tc_stages_dev, tc_u_dev;
   void* pinned = nullptr;        // pinned host staging
   size_t pinned_bytes = 0;
   int64_t last_passes = 0, last_ops = 0, last_bytes = 0;
+  int64_t last_tc_passes = 0, last_tc_blocks = 0, last_tc_swaps = 0;
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
   size_t amp_bytes() const { return (size_t)N * (precision == DMV_C128 ? 16 : 8); }
 };

@@ -20,6 +20,7 @@
 //    run in register phases (phases.cuh), so the tile crosses shared memory
 //    once per phase instead of once per op.
 #include <cuda.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <mutex>
@@ -28,6 +29,7 @@
 #include "internal.h"
 #include "phases.cuh"
 #include "policies.cuh"
+#include "tc.cuh"
 #include "tma.cuh"
 
 namespace dmv {
@@ -513,6 +515,9 @@ int encode_pass_map(CUtensorMap* map, void* amps, int32_t n, const Pass& ps, boo
   return DMV_OK;
 }
 
+// The tensor-core window pass (ARITH_TC) and its launcher.
+#include "tc_window.cuh"
+
 // TMA kernels by policy: register phases for complex64 (FP32 arithmetic),
 // the shared-memory op loop for complex128 in FP64. The complex128 FP32-pair
 // and int64 arithmetics keep the shared-memory kernel (k_apply_window),
@@ -674,11 +679,57 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     phase_ops_dev = static_cast<const PhaseOp*>(s->phase_ops_dev.ptr);
   }
   const Op* ops_dev = static_cast<const Op*>(s->ops_dev.ptr);
+  // Tensor-core arithmetic: the stages and block digit matrices of every
+  // window pass it takes, uploaded once for the whole plan.
+  const bool tc = s->precision == DMV_C128 && s->arith == ARITH_TC;
+  std::vector<int64_t> tc_first(passes.size(), -1);
+  std::vector<int32_t> tc_count(passes.size(), 0);
+  std::vector<int32_t> tc_blocks(passes.size(), 0);
+  if (tc) {
+    s->tc_stages.clear();
+    s->tc_u.clear();
+    for (size_t i = 0; i < passes.size(); ++i) {
+      const Pass& ps = passes[i];
+      if (ps.kind != 1 || !tma_eligible<PolF64>(ps)) continue;
+      const size_t mark = s->tc_stages.size();
+      const size_t umark = s->tc_u.size();
+      if (!build_tc_pass(plan, ps, s->tc_stages, s->tc_u)) continue;
+      tc_first[i] = (int64_t)mark;
+      tc_count[i] = (int32_t)(s->tc_stages.size() - mark);
+      tc_blocks[i] = (int32_t)((s->tc_u.size() - umark) / (size_t)kTcUHalves);
+    }
+    if (!s->tc_stages.empty()) {
+      DMV_TRY(s->tc_stages_dev.reserve(s->tc_stages.size() * sizeof(TcStage)));
+      DMV_CUDA_TRY(cudaMemcpyAsync(s->tc_stages_dev.ptr, s->tc_stages.data(), s->tc_stages.size() * sizeof(TcStage),
+                                   cudaMemcpyHostToDevice, s->stream));
+    }
+    if (!s->tc_u.empty()) {
+      DMV_TRY(s->tc_u_dev.reserve(s->tc_u.size() * sizeof(uint16_t)));
+      DMV_CUDA_TRY(cudaMemcpyAsync(s->tc_u_dev.ptr, s->tc_u.data(), s->tc_u.size() * sizeof(uint16_t),
+                                   cudaMemcpyHostToDevice, s->stream));
+    }
+  }
   int64_t bytes = 0;
   const int64_t S = (int64_t)s->amp_bytes();
-  for (const Pass& ps : passes) {
+  for (size_t pi = 0; pi < passes.size(); ++pi) {
+    const Pass& ps = passes[pi];
+    if (tc && tc_first[pi] >= 0) {
+      // Tensor-core FLOPs: 34 digit products of a 128 x 64 x 64 real product per
+      // 4096-amplitude tile and block (2 FLOPs per multiply-add).
+      const double flops = (double)tc_blocks[pi] * 34.0 * 2.0 * 64.0 * 64.0 * 128.0 * (double)(s->N >> 12);
+      const int64_t tok = prof_begin(DMV_KERNEL_WINDOW, s->stream, (double)(2 * S), flops);
+      DMV_TRY(launch_window_tc(s->amps, s->n, ps,
+                               static_cast<const TcStage*>(s->tc_stages_dev.ptr) + tc_first[pi], tc_count[pi],
+                               static_cast<const uint16_t*>(s->tc_u_dev.ptr), s->stream));
+      prof_end(tok, s->stream);
+      bytes += 2 * S;
+      count_launch();
+      continue;
+    }
     // Block fixed point needs unitary ops; a pass with any other op runs in FP64.
+    // Passes the tensor cores do not take run in the integer-pipe arithmetic.
     int arith = s->precision == DMV_C64 ? ARITH_FP64 : s->arith;
+    if (arith == ARITH_TC) arith = ARITH_INT64;
     if (arith == ARITH_INT64)
       for (int64_t o = 0; o < ps.op_count; ++o)
         if (!plan.ops[(size_t)(ps.op_begin + o)].unitary) arith = ARITH_FP64;
@@ -709,6 +760,13 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     count_launch();
   }
   DMV_CUDA_TRY(cudaGetLastError());
+  s->last_tc_passes = s->last_tc_blocks = s->last_tc_swaps = 0;
+  for (size_t pi = 0; pi < passes.size(); ++pi)
+    if (tc && tc_first[pi] >= 0) {
+      ++s->last_tc_passes;
+      s->last_tc_blocks += tc_blocks[pi];
+      s->last_tc_swaps += tc_count[pi] - tc_blocks[pi];
+    }
   s->last_passes = (int64_t)passes.size();
   s->last_ops = (int64_t)plan.ops.size();
   s->last_bytes = bytes;

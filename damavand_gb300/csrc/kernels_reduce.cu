@@ -568,7 +568,7 @@ int launch_adjoint_step_impl(dmv_state_s* psi, dmv_state_s* lam, const Op& op, i
   if (psi->precision == DMV_C64)
     k_adjoint_step<PolF32><<<grid, kRedThreads, 0, psi->stream>>>(
         static_cast<float2*>(psi->amps), static_cast<float2*>(lam->amps), pairs, op, apply, partial_slot);
-  else if (psi->arith == ARITH_INT64 && op.unitary)
+  else if ((psi->arith == ARITH_INT64 || psi->arith == ARITH_TC) && op.unitary)
     k_adjoint_step<PolFX><<<grid, kRedThreads, 0, psi->stream>>>(
         static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
   else if (psi->arith == ARITH_FP32X2)

@@ -61,8 +61,16 @@ enum { DMV_C128 = 0, DMV_C64 = 1 };
  * DMV_ARITH_INT64: each tile (or pair) is converted to int64 fixed point with
  *   one shared exponent (54 fraction bits for its largest components) and
  *   multiplied exactly in 31-bit limbs on the integer pipe, with one rounding
- *   per output. Passes holding a non-unitary matrix fall back to FP64. */
-enum { DMV_ARITH_FP64 = 0, DMV_ARITH_FP32X2 = 1, DMV_ARITH_INT64 = 2 };
+ *   per output. Passes holding a non-unitary matrix fall back to FP64.
+ * DMV_ARITH_TC: the same int64 block fixed point, but each fused window pass
+ *   is cut into dense blocks (the product of its gates on up to 5 qubits, one
+ *   32 x 32 unitary) and exchanges (X, CNOT). A block is applied to 128
+ *   columns of the tile at once as exact products of balanced 8-bit digits
+ *   (7 per 56-bit integer, FP16) on the tensor cores (tcgen05.mma, FP32
+ *   accumulators in tensor memory, every sum exact), rounded once per
+ *   output. Passes it does not take run as DMV_ARITH_INT64. Single states
+ *   only (batches accept FP64, FP32X2 and INT64). */
+enum { DMV_ARITH_FP64 = 0, DMV_ARITH_FP32X2 = 1, DMV_ARITH_INT64 = 2, DMV_ARITH_TC = 3 };
 
 /* Gate kinds (numbering shared with the oracle). DMV_GATE_MATRIX takes an
  * explicit 2x2 matrix; every kind may carry a control qubit. */
@@ -165,6 +173,10 @@ int dmv_apply_matrix(dmv_state_t s, const double m_re[4], const double m_im[4],
 int dmv_apply_gates(dmv_state_t s, const dmv_gate_t* gates, int64_t num_gates, int32_t fusion);
 /* Number of HBM passes the last dmv_apply_gates call used (plan statistics). */
 int dmv_last_plan_stats(int64_t* num_passes, int64_t* num_fused_ops, int64_t* bytes_moved);
+/* Tensor-core statistics of the last dmv_apply_gates call on a state with
+ * DMV_ARITH_TC: window passes that ran on the tensor cores, their dense
+ * blocks and their exchange stages (zeros for other arithmetics). */
+int dmv_last_tc_stats(dmv_state_t s, int64_t* tc_passes, int64_t* blocks, int64_t* exchanges);
 /* Plans a gate list without touching a GPU (host only): the number of HBM
  * passes, of window passes, of ops after merging, and the largest number of
  * local qubits of a window. tile_bits 0 picks the default for the precision. */
@@ -251,6 +263,11 @@ int dmv_batch_debug_wait_limit(dmv_batch_t b, int64_t spin_limit, int32_t poison
 /* Test hook: the next `count` device allocations of the library fail (as if
  * out of memory). */
 int dmv_debug_fail_allocations(int32_t count);
+/* Test hook: mode 1 makes every dense block of later DMV_ARITH_TC passes read
+ * its tensor-memory accumulators with the exact float-to-integer conversion
+ * instead of the magic-number addition the planner picks when every
+ * accumulator provably stays below 2^22; mode 0 restores the choice. */
+int dmv_debug_tc_convert(int32_t mode);
 /* Test hook: the number of polls after which a TMA window pass stops waiting
  * for a tile load (negative: the default). The pass then drains its copies,
  * leaves the state undefined and the next dmv_state_synchronize returns
