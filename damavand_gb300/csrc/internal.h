@@ -209,7 +209,8 @@ struct TcStage {
   int32_t gctrl;    // swap: control qubit outside the tile, or -1
   int32_t u_index;  // block: index of its digit matrix in the plan's array
   int32_t magic;    // block: 1 when every FP32 accumulator stays below 2^22 in magnitude
-  int32_t pad[3];
+  int32_t next_u;   // block: u_index of the pass's next block (cyclically), fetched during this one's epilogue
+  int32_t pad[2];
 };
 static_assert(sizeof(TcStage) == 48, "TcStage layout");
 

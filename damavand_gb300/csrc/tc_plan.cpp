@@ -91,6 +91,7 @@ bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stage
     if (!ops[i].unitary) return false;
     if (ops[i].ctrl_kind == CTRL_GLOBAL && ops[i].cls != OP_SWAP) return false;
   }
+  const size_t first_stage = stages.size();
   std::vector<int64_t> rem(count), keep, take;
   for (int64_t i = 0; i < count; ++i) rem[i] = i;
   std::vector<double> ur(32 * 32), ui(32 * 32);
@@ -175,6 +176,12 @@ bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stage
     }
     rem.swap(keep);
   }
+  // each block names the digit matrix of the pass's next block, cyclically
+  std::vector<size_t> blocks;
+  for (size_t i = first_stage; i < stages.size(); ++i)
+    if (stages[i].kind == TC_BLOCK) blocks.push_back(i);
+  for (size_t b = 0; b < blocks.size(); ++b)
+    stages[blocks[b]].next_u = stages[blocks[(b + 1) % blocks.size()]].u_index;
   return true;
 }
 

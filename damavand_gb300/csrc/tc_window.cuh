@@ -2,24 +2,25 @@
 // kernels_apply.cu inside its anonymous namespace, after TileGeom and
 // encode_pass_map.
 //
-// One persistent CTA of 128 threads per SM (it holds all 512 TMEM columns and
-// 209 KB of shared memory). Per 2^12-amplitude tile:
+// One persistent CTA of 512 threads per SM (it holds all 512 TMEM columns and
+// 217 KB of shared memory). Per 2^12-amplitude tile:
 //  1. The tile arrives by TMA (the FP64 5-D tensor map of the pass, two tile
 //     buffers: the next tile loads while this one computes) and is converted
 //     in place to int64 block fixed point with the tile's largest exponent
-//     (54 fraction bits, as the integer-pipe arithmetic). Amplitude l sits at
+//     (56 fraction bits, tc_from_double). Amplitude l sits at
 //     l ^ ((l >> 5) & 7), which keeps the column gathers below free of
 //     bank conflicts.
 //  2. Exchange stages swap amplitude pairs in shared memory.
-//  3. A block stage views the tile as 128 columns x 32 block rows. Thread t
-//     gathers column t, scales it so its largest component is below 2^54,
-//     and writes its 7 balanced 8-bit digits (FP16) as row t of a 128 x 64
-//     operand, one digit at a time into two alternating buffers. After each
+//  3. A block stage views the tile as 128 columns x 32 block rows. Threads
+//     t, t + 128, t + 256, t + 384 gather quarters of column t, scale it so its largest
+//     component is below 2^54, and write its 7 balanced 8-bit digits (FP16)
+//     as row t of a 128 x 64 operand, one digit at a time into two
+//     alternating buffers. After each
 //     digit one thread issues the MMAs of that digit against the block's
 //     stacked digit matrix (loaded by a bulk copy), N-stacked so one MMA
 //     covers several matrix digits: digit product (i, j) accumulates into
 //     TMEM columns 64(i+j) .. 64(i+j)+63 (exact: every sum stays below 2^24).
-//     Thread t then reads TMEM lane t, recombines the 8 accumulators into
+//     The same threads then read TMEM lane t, recombine the 8 accumulators into
 //     int64 (sum of D_s 2^(42-8s), rounded once), undoes its column scale
 //     and writes the column back.
 //  4. The tile goes back to FP64 and out by TMA.
@@ -27,7 +28,7 @@
 // the copies and MMAs in flight and ends the kernel.
 // (cuda_fp16.h and tc.cuh are included by the including file.)
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 512;
 constexpr uint32_t kTcTileBytes = 4096u * 16u;               // 64 KB
 constexpr uint32_t kTcDigitBytes = 128u * 64u * 2u;          // one digit of the 128 x 64 operand
 constexpr uint32_t kTcUBytes = (uint32_t)kTcUHalves * 2u;    // 56 KB
@@ -44,6 +45,24 @@ struct TcPassParams {
   const TcStage* stages;
   const uint16_t* u;
 };
+
+// Tile fixed point: with e the tile's largest biased FP64 exponent, x becomes
+// X = round(x * 2^(1078 - e)), so the largest components have 56 fraction
+// bits and |X| < 2^56. A unitary on a 4096-amplitude tile can concentrate its
+// norm on one amplitude, at most 2^6 times the largest component: every value
+// stays below 2^62.
+__device__ __forceinline__ long long tc_from_double(double x, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7FFull);
+  if (E == 0) return 0;  // zero or subnormal: flushed
+  const unsigned long long M = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int s = e - E - 3;  // right shift; negative is a left shift by up to 3
+  unsigned long long X;
+  if (s <= 0) X = M << (-s);
+  else if (s < 63) X = (M + (1ull << (s - 1))) >> s;
+  else X = 0;
+  return (b >> 63) ? -(long long)X : (long long)X;
+}
 
 // Position of tile amplitude l in shared memory.
 __device__ __forceinline__ int tc_pos(int l) { return l ^ ((l >> 5) & 7); }
@@ -83,17 +102,37 @@ __device__ __forceinline__ long long tc_unscale(long long y, int ls) {
   return y << (-ls);
 }
 
-// Recombines output o of one TMEM chunk: sum_s D_s 2^(42-8s), rounded at 2^0.
+// bits(x + 1.5 * 2^23) = kTcMagic + x for an integer |x| < 2^22.
+constexpr int kTcMagic = 0x4B400000;
+// kTcMagic * (2^42 + 2^34 + 2^26 + 2^18 + 2^10 + 2^2) modulo 2^64.
+constexpr unsigned long long kTcMagicSum =
+    (unsigned long long)kTcMagic * ((1ull << 42) + (1ull << 34) + (1ull << 26) + (1ull << 18) + (1ull << 10) + (1ull << 2));
+
+// An FP32 accumulator (an exact integer D) as kTcMagic + D: the magic-number
+// addition when |D| < 2^22 is known, the conversion instruction otherwise.
+template <bool MAGIC>
+__device__ __forceinline__ unsigned tc_acc_biased(uint32_t bits) {
+  if constexpr (MAGIC) return (unsigned)__float_as_int(__fadd_rn(__uint_as_float(bits), 12582912.0f));
+  else return (unsigned)(__float2int_rn(__uint_as_float(bits)) + kTcMagic);
+}
+
+// Output o of one TMEM chunk: sum_s D_s 2^(42-8s), rounded at 2^0. Groups
+// 0..5 are integer terms, summed modulo 2^64 from the biased values (the
+// true sum fits in int64, so the bias can be removed at once); groups 6 and
+// 7 are the fraction, rounded from their exact 32-bit sum.
 template <bool MAGIC>
 __device__ __forceinline__ long long tc_combine(const uint32_t (&g)[8][8], int o) {
-  int c[8];
+  unsigned b[8];
 #pragma unroll
-  for (int s = 0; s < 8; ++s) {
-    if constexpr (MAGIC) c[s] = __float_as_int(__fadd_rn(__uint_as_float(g[s][o]), 12582912.0f)) - 0x4B400000;
-    else c[s] = __float2int_rn(__uint_as_float(g[s][o]));
-  }
-  const int p01 = c[0] * 256 + c[1], p23 = c[2] * 256 + c[3], p45 = c[4] * 256 + c[5], p67 = c[6] * 256 + c[7];
-  return ((long long)p01 << 34) + ((long long)p23 << 18) + ((long long)p45 << 2) + (((long long)p67 + 8192) >> 14);
+  for (int s = 0; s < 8; ++s) b[s] = tc_acc_biased<MAGIC>(g[s][o]);
+  const int low = (int)(b[6] * 256u + b[7] + (8192u - 257u * (unsigned)kTcMagic));  // D_6 2^8 + D_7 + 2^13
+  unsigned long long u = (unsigned long long)(long long)(low >> 14) - kTcMagicSum;
+  u += (unsigned long long)b[5] * 4ull;
+  u += (unsigned long long)b[4] * 1024ull;
+  u += (unsigned long long)b[3] * 262144ull;
+  u += (unsigned long long)b[2] * 67108864ull;
+  u += (unsigned long long)(b[1] * 4u + b[0] * 1024u) << 32;
+  return (long long)u;
 }
 
 __device__ __forceinline__ void tc_issue_digit(int digit, uint32_t tbase, uint32_t a_addr, uint32_t u_addr) {
@@ -111,37 +150,103 @@ __device__ __forceinline__ void tc_issue_digit(int digit, uint32_t tbase, uint32
   }
 }
 
-// Gathers column `basem` of a block, computes its digits, runs the MMAs and
-// writes the column back. Returns false if a wait gave up (uniform over the CTA).
+// Block row r (0..31) of a column as tile bits.
+__device__ __forceinline__ int tc_dep(int r, const int (&d)[5]) {
+  return ((r & 1) ? d[0] : 0) | ((r & 2) ? d[1] : 0) | ((r & 4) ? d[2] : 0) | ((r & 8) ? d[3] : 0) |
+         ((r & 16) ? d[4] : 0);
+}
+
+// Thread (h, m) reads TMEM lane m, outputs 16h .. 16h+15 (block rows
+// 8h .. 8h+7, at shared-memory positions pos[]), and writes them back.
 template <bool MAGIC>
-__device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, int basem, unsigned char* adig0,
-                                         unsigned char* adig1, unsigned char* ubuf, uint32_t tbase, uint32_t tlane,
-                                         uint64_t* s_afree, uint64_t* s_acc, uint64_t* s_ufull, uint32_t& n_afree0,
-                                         uint32_t& n_afree1, uint32_t& n_acc, bool u_wait, uint32_t n_u,
-                                         uint32_t limit) {
-  const int tid = threadIdx.x;
-  const int d0 = 1 << st.bits[0], d1 = 1 << st.bits[1], d2 = 1 << st.bits[2], d3 = 1 << st.bits[3],
-            d4 = 1 << st.bits[4];
-  longlong2 v[32];
+__device__ __forceinline__ void tc_epilogue(longlong2* tile, const int (&pos)[8], int h, int ls, uint32_t tlane) {
+#pragma unroll 1
+  for (int c = 0; c < 2; ++c) {
+    const int q = 2 * h + c;
+    uint32_t g[8][8];
 #pragma unroll
-  for (int r = 0; r < 32; ++r) {
-    const int dep = ((r & 1) ? d0 : 0) | ((r & 2) ? d1 : 0) | ((r & 4) ? d2 : 0) | ((r & 8) ? d3 : 0) |
-                    ((r & 16) ? d4 : 0);
-    v[r] = tile[tc_pos(basem | dep)];
+    for (int s = 0; s < 8; ++s) tc_ld8(tlane + (uint32_t)(64 * s + 8 * q), g[s]);
+    tc_wait_ld();
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      longlong2 o;
+      o.x = tc_unscale(tc_combine<MAGIC>(g, 2 * a), ls);
+      o.y = tc_unscale(tc_combine<MAGIC>(g, 2 * a + 1), ls);
+      tile[c ? pos[4 + a] : pos[a]] = o;
+    }
   }
+}
+
+// Waits for phase `parity` of `bar`, each poll suspending the thread in
+// hardware for up to ~0.5 us (no busy polling); gives up after `limit` polls.
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity), "r"(500u)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Per-CTA progress of the barriers and the digit-matrix buffer (identical in
+// every thread).
+struct TcSync {
+  uint32_t n_afree0 = 0, n_afree1 = 0, n_acc = 0, n_u = 0;
+  int u_issued = -1;  // digit matrix of the last bulk copy into the buffer
+  bool u_ready = true;
+};
+
+// One dense block on the tile. Returns false if a wait gave up (uniform over
+// the CTA). Thread (h, m) = (tid / 128, tid % 128) owns block rows 8h .. 8h+7
+// of column m: it gathers them, writes their digits (K columns 16h .. 16h+15
+// of row m) and, from TMEM lane m, their 16 outputs. The threads publish
+// each digit by arriving on s_afull; thread 0 waits there and issues that
+// digit's MMAs, so the other threads never wait for each other until the
+// epilogue.
+__device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, const TcPassParams& p, int basem,
+                                         unsigned char* adig0, unsigned char* adig1, unsigned char* ubuf,
+                                         uint32_t tbase, uint32_t tlane, uint64_t* s_afull, uint64_t* s_afree,
+                                         uint64_t* s_acc, uint64_t* s_ufull, unsigned long long* s_cmax, TcSync& sy) {
+  const int tid = threadIdx.x, h = tid >> 7, m = tid & 127;
+  const uint32_t limit = p.wait_limit;
+  const int d[5] = {1 << st.bits[0], 1 << st.bits[1], 1 << st.bits[2], 1 << st.bits[3], 1 << st.bits[4]};
+  if (st.u_index != sy.u_issued) {  // the first block of this CTA (later ones are prefetched)
+    if (tid == 0) {
+      mbar_arrive_expect_tx(s_ufull, kTcUBytes);
+      bulk_load(ubuf, p.u + (size_t)st.u_index * (size_t)kTcUHalves, kTcUBytes, s_ufull);
+    }
+    sy.u_issued = st.u_index;
+    ++sy.n_u;
+    sy.u_ready = false;
+  }
+  // gather block rows 8h .. 8h+7 of column m; the column's scale (the bit
+  // length of its largest one's-complement magnitude)
+  int pos[8];
+  longlong2 v[8];
   unsigned long long mx = 0;
 #pragma unroll
-  for (int r = 0; r < 32; ++r) {
-    const long long x = v[r].x, y = v[r].y;
-    mx |= (unsigned long long)((x ^ (x >> 63)) - (x >> 63)) | (unsigned long long)((y ^ (y >> 63)) - (y >> 63));
+  for (int j = 0; j < 8; ++j) {
+    pos[j] = tc_pos(basem | tc_dep(8 * h + j, d));
+    v[j] = tile[pos[j]];
+    mx |= (unsigned long long)(v[j].x ^ (v[j].x >> 63)) | (unsigned long long)(v[j].y ^ (v[j].y >> 63));
   }
+  s_cmax[tid] = mx;
+  __syncthreads();
+  mx = s_cmax[m] | s_cmax[m + 128] | s_cmax[m + 256] | s_cmax[m + 384];
   const int bl = mx ? 64 - __clzll((long long)mx) : 0;
   const int ls = mx ? 54 - bl : 0;
   constexpr unsigned long long kBias = 0x0080808080808080ull;
 #pragma unroll
-  for (int r = 0; r < 32; ++r) {
-    v[r].x = (long long)((unsigned long long)tc_scale(v[r].x, ls) + kBias);
-    v[r].y = (long long)((unsigned long long)tc_scale(v[r].y, ls) + kBias);
+  for (int j = 0; j < 8; ++j) {
+    v[j].x = (long long)((unsigned long long)tc_scale(v[j].x, ls) + kBias);
+    v[j].y = (long long)((unsigned long long)tc_scale(v[j].y, ls) + kBias);
   }
   const uint32_t u_addr = (uint32_t)__cvta_generic_to_shared(ubuf);
   bool ok = true;
@@ -149,12 +254,12 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, int
   for (int i = 0; i < kTcDigits; ++i) {
     const int ab = i & 1;
     unsigned char* const abuf = ab ? adig1 : adig0;
-    if (i >= 2) ok = mbar_wait(&s_afree[ab], ((ab ? n_afree1 : n_afree0) - 1) & 1u, limit);
-    if (i == 0 && u_wait) ok = mbar_wait(s_ufull, (n_u - 1) & 1u, limit);
-    unsigned char* row = abuf + (size_t)(tid >> 3) * 1024 + (size_t)(tid & 7) * 16;
+    const uint32_t k = ab ? sy.n_afree1 : sy.n_afree0;  // earlier digits written into this buffer
+    if (i >= 2) ok &= tc_wait(&s_afree[ab], (k - 1) & 1u, limit);
+    unsigned char* row = abuf + (size_t)(m >> 3) * 1024 + (size_t)(m & 7) * 16 + (size_t)h * 256;
     const int byte = kTcDigits - 1 - i;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
+    for (int c = 0; c < 2; ++c) {
       uint4 w;
       w.x = tc_digit_pair((uint64_t)v[4 * c + 0].x, (uint64_t)v[4 * c + 0].y, byte);
       w.y = tc_digit_pair((uint64_t)v[4 * c + 1].x, (uint64_t)v[4 * c + 1].y, byte);
@@ -163,37 +268,40 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, int
       if (ok) *reinterpret_cast<uint4*>(row + (size_t)c * 128) = w;
     }
     fence_proxy_async_smem();
-    if (__syncthreads_or(!ok)) return false;
+    mbar_arrive(&s_afull[ab]);
     if (tid == 0) {
-      tc_fence_after_sync();
-      tc_issue_digit(i, tbase, (uint32_t)__cvta_generic_to_shared(abuf), u_addr);
+      // the issuing thread polls (a suspended wait would delay the MMAs)
+      bool go = ok && mbar_wait(&s_afull[ab], k & 1u, limit);
+      if (i == 0 && !sy.u_ready) go = go && mbar_wait(s_ufull, (sy.n_u - 1) & 1u, limit);
+      if (go) {
+        tc_fence_after_sync();
+        tc_issue_digit(i, tbase, (uint32_t)__cvta_generic_to_shared(abuf), u_addr);
+      }
+      ok = go;
+      // commits arrive even after a failure, so no thread waits on them forever
       tc_commit(&s_afree[ab]);
       if (i == kTcDigits - 1) tc_commit(s_acc);
     }
-    if (ab) ++n_afree1;
-    else ++n_afree0;
+    if (ab) ++sy.n_afree1;
+    else ++sy.n_afree0;
   }
-  ++n_acc;
-  ok = mbar_wait(s_acc, (n_acc - 1) & 1u, limit);
+  sy.u_ready = true;
+  ++sy.n_acc;
+  ok &= tc_wait(s_acc, (sy.n_acc - 1) & 1u, limit);
   if (__syncthreads_or(!ok)) return false;
   tc_fence_after_sync();
-#pragma unroll 1
-  for (int q = 0; q < 8; ++q) {
-    uint32_t g[8][8];
-#pragma unroll
-    for (int s = 0; s < 8; ++s) tc_ld8(tlane + (uint32_t)(64 * s + 8 * q), g[s]);
-    tc_wait_ld();
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int r = 4 * q + a;
-      const int dep = ((r & 1) ? d0 : 0) | ((r & 2) ? d1 : 0) | ((r & 4) ? d2 : 0) | ((r & 8) ? d3 : 0) |
-                      ((r & 16) ? d4 : 0);
-      longlong2 o;
-      o.x = tc_unscale(tc_combine<MAGIC>(g, 2 * a), ls);
-      o.y = tc_unscale(tc_combine<MAGIC>(g, 2 * a + 1), ls);
-      tile[tc_pos(basem | dep)] = o;
+  // the MMAs have read the digit matrix: fetch the pass's next one during the epilogue
+  if (st.next_u != sy.u_issued) {
+    if (tid == 0) {
+      mbar_arrive_expect_tx(s_ufull, kTcUBytes);
+      bulk_load(ubuf, p.u + (size_t)st.next_u * (size_t)kTcUHalves, kTcUBytes, s_ufull);
     }
+    sy.u_issued = st.next_u;
+    ++sy.n_u;
+    sy.u_ready = false;
   }
+  if (st.magic) tc_epilogue<true>(tile, pos, h, ls, tlane);
+  else tc_epilogue<false>(tile, pos, h, ls, tlane);
   tc_fence_before_sync();
   __syncthreads();
   return true;
@@ -203,12 +311,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TcPassParams p) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t s_full[2];
+  __shared__ __align__(8) uint64_t s_afull[2];
   __shared__ __align__(8) uint64_t s_afree[2];
   __shared__ __align__(8) uint64_t s_acc;
   __shared__ __align__(8) uint64_t s_ufull;
   __shared__ uint32_t s_tbase;
   __shared__ int s_red[kTcThreads / 32];
   __shared__ int s_high[16];
+  __shared__ unsigned long long s_cmax[kTcThreads];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* const adig0 = base + 2 * kTcTileBytes;
@@ -220,6 +330,8 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
   if (tid == 0) {
     mbar_init(&s_full[0], 1);
     mbar_init(&s_full[1], 1);
+    mbar_init(&s_afull[0], kTcThreads);
+    mbar_init(&s_afull[1], kTcThreads);
     mbar_init(&s_afree[0], 1);
     mbar_init(&s_afree[1], 1);
     mbar_init(&s_acc, 1);
@@ -231,49 +343,52 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
   __syncthreads();
   tc_fence_after_sync();
   const uint32_t tbase = s_tbase;
-  const uint32_t tlane = tbase + ((uint32_t)(warp * 32) << 16);
+  // warp w reads TMEM lanes 32 (w % 4) .. +31: the lanes of columns tid % 128
+  const uint32_t tlane = tbase + ((uint32_t)((warp & 3) * 32) << 16);
   const TileGeom<16> geom{p.low, p.nh, s_high};
   const uint32_t limit = p.wait_limit;
-  uint32_t n_afree0 = 0u, n_afree1 = 0u, n_acc = 0u, n_u = 0u;
-  int u_resident = -1;
+  TcSync sy;
   bool failed = false;
   // loads issued into each tile buffer, and whether the last one is not yet consumed
-  uint32_t n_load[2] = {0u, 0u};
-  bool pending[2] = {false, false};
+  uint32_t n_load0 = 0u, n_load1 = 0u;
+  bool pending0 = false, pending1 = false;
   int64_t tix = blockIdx.x;
   if (tix < p.num_tiles) {
     if (warp == 0) geom.load(&tmap, &s_full[0], base, tix, p.boxes, kTcTileBytes, lane);
-    ++n_load[0];
-    pending[0] = true;
+    ++n_load0;
+    pending0 = true;
   }
   for (int64_t it = 0; tix < p.num_tiles; ++it, tix += gridDim.x) {
     const int buf = (int)(it & 1);
     unsigned char* const tbytes = buf ? base + kTcTileBytes : base;
     unsigned char* const tother = buf ? base : base + kTcTileBytes;
     longlong2* tile = reinterpret_cast<longlong2*>(tbytes);
-    const bool ok = mbar_wait(&s_full[buf], (n_load[buf] - 1) & 1u, limit);
+    const bool ok = tc_wait(&s_full[buf], ((buf ? n_load1 : n_load0) - 1) & 1u, limit);
     if (__syncthreads_or(!ok)) {
       failed = true;
       break;
     }
-    pending[buf] = false;
+    if (buf) pending1 = false;
+    else pending0 = false;
     // FP64 -> int64 block fixed point, in place, at the swizzled positions
-    double2 d[32];
+    double2 dd[8];
     const double2* td = reinterpret_cast<const double2*>(tile);
     unsigned emax = 0;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      d[j] = td[tid + 128 * j];
-      emax = max(emax, (unsigned)max(fx_exponent(d[j].x), fx_exponent(d[j].y)));
+    for (int j = 0; j < 8; ++j) {
+      dd[j] = td[tid + kTcThreads * j];
+      emax = max(emax, (unsigned)max(fx_exponent(dd[j].x), fx_exponent(dd[j].y)));
     }
     emax = __reduce_max_sync(0xffffffffu, emax);
     if (lane == 0) s_red[warp] = (int)emax;
     __syncthreads();
-    const int e = max(max(s_red[0], s_red[1]), max(s_red[2], s_red[3]));
+    int e = 0;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int l = tid + 128 * j;
-      tile[tc_pos(l)] = make_longlong2(fx_from_double(d[j].x, e), fx_from_double(d[j].y, e));
+    for (int w = 0; w < kTcThreads / 32; ++w) e = max(e, s_red[w]);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int l = tid + kTcThreads * j;
+      tile[tc_pos(l)] = make_longlong2(tc_from_double(dd[j].x, e), tc_from_double(dd[j].y, e));
     }
     __syncthreads();
     // the next tile loads into the other buffer once that buffer's store has drained
@@ -283,8 +398,13 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
         tma_wait_group_read<0>();
         geom.load(&tmap, &s_full[buf ^ 1], tother, next, p.boxes, kTcTileBytes, lane);
       }
-      ++n_load[buf ^ 1];
-      pending[buf ^ 1] = true;
+      if (buf) {
+        ++n_load0;
+        pending0 = true;
+      } else {
+        ++n_load1;
+        pending1 = true;
+      }
     }
     const int64_t tile_base = geom.base(tix);
     for (int si = 0; si < p.num_stages; ++si) {
@@ -293,9 +413,9 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
         if (st.gctrl >= 0 && !((tile_base >> st.gctrl) & 1)) continue;
         const int tb = st.bits[0], cb = st.bits[1];
         if (cb < 0) {
-#pragma unroll 4
-          for (int j = 0; j < 16; ++j) {
-            const int l0 = tc_insert_zero(tid + 128 * j, tb), l1 = l0 | (1 << tb);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int l0 = tc_insert_zero(tid + kTcThreads * j, tb), l1 = l0 | (1 << tb);
             const int p0 = tc_pos(l0), p1 = tc_pos(l1);
             const longlong2 a0 = tile[p0], a1 = tile[p1];
             tile[p0] = a1;
@@ -303,9 +423,10 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
           }
         } else {
           const int lo = min(tb, cb), hi = max(tb, cb);
-#pragma unroll 4
-          for (int j = 0; j < 8; ++j) {
-            const int l0 = tc_insert_zero(tc_insert_zero(tid + 128 * j, lo), hi) | (1 << cb), l1 = l0 | (1 << tb);
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const int l0 = tc_insert_zero(tc_insert_zero(tid + kTcThreads * j, lo), hi) | (1 << cb);
+            const int l1 = l0 | (1 << tb);
             const int p0 = tc_pos(l0), p1 = tc_pos(l1);
             const longlong2 a0 = tile[p0], a1 = tile[p1];
             tile[p0] = a1;
@@ -318,26 +439,15 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
       // dense block: the 7 tile bits outside it index the 128 columns
       const uint32_t bmask = (1u << st.bits[0]) | (1u << st.bits[1]) | (1u << st.bits[2]) | (1u << st.bits[3]) |
                              (1u << st.bits[4]);
+      const int m = tid & 127;
       int basem = 0;
       for (int b = 0, c = 0; b < 12; ++b)
         if (!(bmask & (1u << b))) {
-          basem |= ((tid >> c) & 1) << b;
+          basem |= ((m >> c) & 1) << b;
           ++c;
         }
-      const bool u_wait = st.u_index != u_resident;
-      if (u_wait) {
-        if (tid == 0) {
-          mbar_arrive_expect_tx(&s_ufull, kTcUBytes);
-          bulk_load(ubuf, p.u + (size_t)st.u_index * (size_t)kTcUHalves, kTcUBytes, &s_ufull);
-        }
-        u_resident = st.u_index;
-        ++n_u;
-      }
-      const bool okb = st.magic ? tc_block<true>(tile, st, basem, adig0, adig1, ubuf, tbase, tlane, s_afree, &s_acc,
-                                                 &s_ufull, n_afree0, n_afree1, n_acc, u_wait, n_u, limit)
-                                : tc_block<false>(tile, st, basem, adig0, adig1, ubuf, tbase, tlane, s_afree, &s_acc,
-                                                  &s_ufull, n_afree0, n_afree1, n_acc, u_wait, n_u, limit);
-      if (!okb) {
+      if (!tc_block(tile, st, p, basem, adig0, adig1, ubuf, tbase, tlane, s_afull, s_afree, &s_acc, &s_ufull, s_cmax,
+                    sy)) {
         failed = true;
         break;
       }
@@ -345,14 +455,14 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
     if (failed) break;
     // int64 -> FP64, back to the linear layout, out by TMA
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const longlong2 x = tile[tc_pos(tid + 128 * j)];
-      d[j] = make_double2(fx_to_double(x.x, e), fx_to_double(x.y, e));
+    for (int j = 0; j < 8; ++j) {
+      const longlong2 x = tile[tc_pos(tid + kTcThreads * j)];
+      dd[j] = make_double2(fx_to_double(x.x, e - 2), fx_to_double(x.y, e - 2));  // X * 2^(e - 1078)
     }
     __syncthreads();
     double2* tw = reinterpret_cast<double2*>(tile);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) tw[tid + 128 * j] = d[j];
+    for (int j = 0; j < 8; ++j) tw[tid + kTcThreads * j] = dd[j];
     fence_proxy_async_smem();
     __syncthreads();
     if (warp == 0) geom.store(&tmap, tbytes, tix, p.boxes, kTcTileBytes, lane);
@@ -362,13 +472,16 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
       atomicExch(p.status, 1);
       // every MMA issued so far completes before the TMEM is released
       tc_commit(&s_acc);
-      mbar_wait(&s_acc, n_acc & 1u, kTmaDrainLimit);
+      mbar_wait(&s_acc, sy.n_acc & 1u, kTmaDrainLimit);
+      if (sy.n_u > 0) mbar_wait(&s_ufull, (sy.n_u - 1) & 1u, kTmaDrainLimit);  // the last digit-matrix copy
     }
     if (warp == 0) {
       // loads in flight land before the CTA's shared memory is released
-      for (int b = 0; b < 2; ++b)
-        if (pending[b]) mbar_wait(&s_full[b], (n_load[b] - 1) & 1u, kTmaDrainLimit);
+      if (pending0) mbar_wait(&s_full[0], (n_load0 - 1) & 1u, kTmaDrainLimit);
+      if (pending1) mbar_wait(&s_full[1], (n_load1 - 1) & 1u, kTmaDrainLimit);
     }
+  } else if (!sy.u_ready && tid == 0) {
+    mbar_wait(&s_ufull, (sy.n_u - 1) & 1u, kTmaDrainLimit);  // a prefetched digit matrix still landing
   }
   if (warp == 0) tma_wait_group_all();
   tc_fence_before_sync();
