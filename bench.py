@@ -44,7 +44,9 @@ METRIC = "30-qubit gate applies/s + HBM GB/s; adjoint vs param-shift grads/s at 
 UNIT = "gate-applies/s"
 DTYPES = {"fp64": "f64 (complex128 storage and FP64 arithmetic)",
           "fp32x2": "f32x2 (complex128 storage, FP32-pair arithmetic, ~48-bit)",
-          "int64": "int64 (complex128 storage, block fixed point: 54-bit fraction per tile, exact products)"}
+          "int64": "int64 (complex128 storage, block fixed point: 54-bit fraction per tile, exact products)",
+          "tc": "int64 (complex128 storage, block fixed point: 56-bit fraction per tile; fused gates as dense "
+                "5-qubit blocks, exact products of FP16 digits on the tcgen05 tensor cores)"}
 # Integer multiply-add (IMAD) throughput of a GB300 measured with an independent-chain kernel.
 INT_MAD_PEAK_T = 18.85
 # FP64 multiply-add throughput of a GB300 measured with an independent-FMA-chain kernel
@@ -53,12 +55,15 @@ FP64_FMA_PEAK_T = 0.504
 FP32_FMA_PEAK_T = 35.9
 # dram__bytes_read.sum + dram__bytes_write.sum per launch divided by the amplitudes of
 # the captured case (profiles/k_window_tma_fp64_24q_full.md: 479.9 MB at 2^24;
-# profiles/k_window_phases_c64_26q_full.md: 1012.3 MB at 2^26).
+# profiles/k_window_phases_c64_26q_full.md: 1012.3 MB at 2^26;
+# profiles/k_window_tc_24q_full.md: 475.8 MB at 2^24).
 NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 479.873280e6 / (1 << 24),
-                             ("window", "c64"): 1012.291328e6 / (1 << 26)}
+                             ("window", "c64"): 1012.291328e6 / (1 << 26),
+                             ("window", "c128", "tc"): 475.753472e6 / (1 << 24)}
 # The kernel that runs a fused window pass, by arithmetic and precision.
 WINDOW_KERNEL = {("fp64", "c128"): "k_window_tma<PolF64>", ("fp32x2", "c128"): "k_apply_window<PolDF>",
-                 ("int64", "c128"): "k_apply_window<PolFX>", ("fp32", "c64"): "k_window_phases<PolF32>"}
+                 ("int64", "c128"): "k_apply_window<PolFX>", ("tc", "c128"): "k_window_tc",
+                 ("fp32", "c64"): "k_window_phases<PolF32>"}
 
 
 def load_peaks():
@@ -68,6 +73,17 @@ def load_peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def load_tensor_peak():
+    """Dense bf16 tensor throughput (TFLOP/s) sustained over a seconds-long loop: the window
+    passes run back to back inside a multi-second forward."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops_sustained"]), "measured (cuBLAS bf16, sustained)"
+    except Exception:
+        return 1700.0, "fallback (sustained)"
 
 
 class ClockSampler:
@@ -395,6 +411,16 @@ def timed_forward(c, args, world, local):
     return step_ms, read_families(lib, check), launches, clocks.summary(), step
 
 
+def tc_stats(c):
+    """Window passes of the last forward that ran on the tensor cores, their dense blocks and exchanges."""
+    import ctypes
+
+    from damavand_gb300._lib import check, lib
+    p, b, x = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    check(lib.dmv_last_tc_stats(c.state().handle, ctypes.byref(p), ctypes.byref(b), ctypes.byref(x)))
+    return {"passes": p.value, "dense_blocks": b.value, "exchanges": x.value}
+
+
 def rooflines(fam, n, arith, prec="c128"):
     dom = max(fam, key=lambda k: fam[k]["ms"])
     d = fam[dom]
@@ -404,8 +430,9 @@ def rooflines(fam, n, arith, prec="c128"):
     achieved = per_launch_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
     # DRAM bytes per launch from one ncu capture (profiles/*_full.md), scaled by state size.
     traffic = None
-    if (dom, prec) in NCU_TRAFFIC_PER_AMPLITUDE:
-        traffic = NCU_TRAFFIC_PER_AMPLITUDE[(dom, prec)] * (1 << n)
+    key = (dom, prec, arith) if (dom, prec, arith) in NCU_TRAFFIC_PER_AMPLITUDE else (dom, prec)
+    if key in NCU_TRAFFIC_PER_AMPLITUDE:
+        traffic = NCU_TRAFFIC_PER_AMPLITUDE[key] * (1 << n)
     kernel = WINDOW_KERNEL.get((arith, prec), "window") if dom == "window" else f"k_apply_{dom}"
     roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
@@ -416,6 +443,12 @@ def rooflines(fam, n, arith, prec="c128"):
     if arith == "fp64":
         ra = {"bound": "fp64", "achieved": rate, "peak": FP64_FMA_PEAK_T, "unit": "T FMA/s",
               "frac": rate / FP64_FMA_PEAK_T, "peak_source": "measured (FP64 FMA chain kernel on this pool's GB300)"}
+    elif arith == "tc":
+        tpeak, tkind = load_tensor_peak()
+        ra = {"bound": "tensor", "achieved": rate, "peak": tpeak, "unit": "TFLOP/s",
+              "frac": rate / tpeak, "peak_source": tkind,
+              "counts": "FP16 digit-product FLOPs: 34 products of a 128x64x64 real product per 4096-amplitude tile "
+                        "and dense block"}
     elif arith == "int64":
         ra = {"bound": "int-mad", "achieved": rate, "peak": INT_MAD_PEAK_T, "unit": "T IMAD/s",
               "frac": rate / INT_MAD_PEAK_T,
@@ -517,7 +550,7 @@ def run_ours(args, world, rank, local):
     # ---- the other complex128 arithmetics, same workload and protocol, each checked against FP64
     if not args.no_alt:
         import torch
-        alts = [a for a in ("fp64", "fp32x2", "int64") if a != args.arith]
+        alts = [a for a in ("fp64", "fp32x2", "int64", "tc") if a != args.arith]
         out["alt_arithmetic"] = []
         for alt in alts:
             c2 = Circuit(n, "gpu", fusion=not args.no_fusion, arithmetic=alt)
@@ -537,6 +570,8 @@ def run_ours(args, world, rank, local):
                 "arithmetic": alt, "dtype": DTYPES[alt], "value": world * G / (ms2 / 1e3), "unit": UNIT,
                 "ms_per_step": ms2, "roofline": rl2, "roofline_arith": ra2, "hbm_gbs_pass_bytes": gbs2,
                 "gpu_launches": int(launches2), "clocks": clocks2}
+            if alt == "tc":
+                entry["tensor_core_passes"] = tc_stats(c2)
             if err is not None:
                 entry["parity"] = {"against": "the FP64-arithmetic forward of this run", "normwise_max_err": err,
                                    "tolerance": 1e-12, "ok": err <= 1e-12}
@@ -580,9 +615,9 @@ def main():
     ap.add_argument("--no-fusion", action="store_true")
     ap.add_argument("--no-alt", action="store_true",
                     help="skip the other complex128 arithmetics (timed and checked against FP64)")
-    ap.add_argument("--arith", choices=["fp64", "fp32x2", "int64"], default="fp64",
+    ap.add_argument("--arith", choices=["fp64", "fp32x2", "int64", "tc"], default="fp64",
                     help="complex128 arithmetic: IEEE FP64, FP32 pairs (error-free transformations), "
-                         "or int64 block fixed point")
+                         "int64 block fixed point, or the same with dense blocks on the tensor cores")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--workload", choices=["default", "large"], default="default",

@@ -210,7 +210,8 @@ struct TcStage {
   int32_t u_index;  // block: index of its digit matrix in the plan's array
   int32_t magic;    // block: 1 when every FP32 accumulator stays below 2^22 in magnitude
   int32_t next_u;   // block: u_index of the pass's next block (cyclically), fetched during this one's epilogue
-  int32_t pad[2];
+  int32_t cols;     // block: the 7 other tile bits (column index bits 0..6), 4 bits each
+  int32_t pad;
 };
 static_assert(sizeof(TcStage) == 48, "TcStage layout");
 

@@ -169,6 +169,8 @@ bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stage
       std::memset(&st, 0, sizeof(st));
       st.kind = TC_BLOCK;
       for (int b = 0; b < kTcBlockBits; ++b) st.bits[b] = bits[b];
+      for (int b = 0, c = 0; b < k; ++b)
+        if (!(S & (1u << b))) st.cols |= b << (4 * c++);
       st.gctrl = -1;
       st.u_index = (int32_t)(u.size() / (size_t)kTcUHalves);
       st.magic = append_block_digits(ur.data(), ui.data(), u) && g_tc_convert_mode == 0 ? 1 : 0;

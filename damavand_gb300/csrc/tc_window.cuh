@@ -34,6 +34,9 @@ constexpr uint32_t kTcDigitBytes = 128u * 64u * 2u;          // one digit of the
 constexpr uint32_t kTcUBytes = (uint32_t)kTcUHalves * 2u;    // 56 KB
 constexpr size_t kTcSmem = 2 * (size_t)kTcTileBytes + 2 * (size_t)kTcDigitBytes + kTcUBytes + 1024;
 
+// Stages a CTA copies to shared memory (a longer pass reads them from global memory).
+constexpr int kTcSmemStages = 40;
+
 struct TcPassParams {
   int k, low, nh, boxes;
   int high[16];
@@ -91,15 +94,10 @@ __device__ __forceinline__ uint32_t tc_digit_pair(uint64_t a, uint64_t b, int by
   return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-__device__ __forceinline__ long long tc_scale(long long v, int ls) {
-  if (ls >= 0) return v << ls;
-  const int s = -ls;
-  return (v + (1ll << (s - 1))) >> s;
-}
-
-__device__ __forceinline__ long long tc_unscale(long long y, int ls) {
-  if (ls > 0) return (y + (1ll << (ls - 1))) >> ls;
-  return y << (-ls);
+// v * 2^ls, rounded to nearest (ties up) when ls < 0; the same code for
+// both signs (the threads of a warp hold columns with different ls).
+__device__ __forceinline__ long long tc_shift(long long v, int lsl, int lsr, long long rnd) {
+  return ((long long)((unsigned long long)v << lsl) + rnd) >> lsr;
 }
 
 // bits(x + 1.5 * 2^23) = kTcMagic + x for an integer |x| < 2^22.
@@ -114,25 +112,6 @@ template <bool MAGIC>
 __device__ __forceinline__ unsigned tc_acc_biased(uint32_t bits) {
   if constexpr (MAGIC) return (unsigned)__float_as_int(__fadd_rn(__uint_as_float(bits), 12582912.0f));
   else return (unsigned)(__float2int_rn(__uint_as_float(bits)) + kTcMagic);
-}
-
-// Output o of one TMEM chunk: sum_s D_s 2^(42-8s), rounded at 2^0. Groups
-// 0..5 are integer terms, summed modulo 2^64 from the biased values (the
-// true sum fits in int64, so the bias can be removed at once); groups 6 and
-// 7 are the fraction, rounded from their exact 32-bit sum.
-template <bool MAGIC>
-__device__ __forceinline__ long long tc_combine(const uint32_t (&g)[8][8], int o) {
-  unsigned b[8];
-#pragma unroll
-  for (int s = 0; s < 8; ++s) b[s] = tc_acc_biased<MAGIC>(g[s][o]);
-  const int low = (int)(b[6] * 256u + b[7] + (8192u - 257u * (unsigned)kTcMagic));  // D_6 2^8 + D_7 + 2^13
-  unsigned long long u = (unsigned long long)(long long)(low >> 14) - kTcMagicSum;
-  u += (unsigned long long)b[5] * 4ull;
-  u += (unsigned long long)b[4] * 1024ull;
-  u += (unsigned long long)b[3] * 262144ull;
-  u += (unsigned long long)b[2] * 67108864ull;
-  u += (unsigned long long)(b[1] * 4u + b[0] * 1024u) << 32;
-  return (long long)u;
 }
 
 __device__ __forceinline__ void tc_issue_digit(int digit, uint32_t tbase, uint32_t a_addr, uint32_t u_addr) {
@@ -156,10 +135,32 @@ __device__ __forceinline__ int tc_dep(int r, const int (&d)[5]) {
          ((r & 16) ? d[4] : 0);
 }
 
-// Thread (h, m) reads TMEM lane m, outputs 16h .. 16h+15 (block rows
-// 8h .. 8h+7, at shared-memory positions pos[]), and writes them back.
+// Output o of one TMEM chunk: sum_s D_s 2^(42-8s), rounded at 2^0. Groups
+// 0..5 are integer terms, summed modulo 2^64 from the biased values (the
+// true sum fits in int64, so the bias comes off at once); groups 6 and 7 are
+// the fraction, rounded from their exact 32-bit sum D_6 2^8 + D_7.
 template <bool MAGIC>
-__device__ __forceinline__ void tc_epilogue(longlong2* tile, const int (&pos)[8], int h, int ls, uint32_t tlane) {
+__device__ __forceinline__ long long tc_combine(const uint32_t (&g)[8][8], int o) {
+  unsigned b[8];
+#pragma unroll
+  for (int s = 0; s < 8; ++s) b[s] = tc_acc_biased<MAGIC>(g[s][o]);
+  const int low = (int)(b[6] * 256u + b[7] + (8192u - 257u * (unsigned)kTcMagic));  // D_6 2^8 + D_7 + 2^13
+  unsigned long long u = (unsigned long long)(long long)(low >> 14) - kTcMagicSum;
+  u += (unsigned long long)b[5] * 4ull;
+  u += (unsigned long long)b[4] * 1024ull;
+  u += (unsigned long long)b[3] * 262144ull;
+  u += (unsigned long long)b[2] * 67108864ull;
+  u += (unsigned long long)(b[1] * 4u + b[0] * 1024u) << 32;
+  return (long long)u;
+}
+
+// Thread (h, m) reads TMEM lane m, outputs 16h .. 16h+15 (block rows
+// 8h .. 8h+7), undoes the column scale and writes them back.
+template <bool MAGIC>
+__device__ __forceinline__ void tc_epilogue(longlong2* tile, int hbase, int d0, int d1, int d2, int h, int ls,
+                                            uint32_t tlane) {
+  const int lsr = ls > 0 ? ls : 0, lsl = ls < 0 ? -ls : 0;
+  const long long rnd = lsr ? (1ll << (lsr - 1)) : 0;
 #pragma unroll 1
   for (int c = 0; c < 2; ++c) {
     const int q = 2 * h + c;
@@ -167,12 +168,12 @@ __device__ __forceinline__ void tc_epilogue(longlong2* tile, const int (&pos)[8]
 #pragma unroll
     for (int s = 0; s < 8; ++s) tc_ld8(tlane + (uint32_t)(64 * s + 8 * q), g[s]);
     tc_wait_ld();
+    const int cbase = hbase | (c ? d2 : 0);
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      longlong2 o;
-      o.x = tc_unscale(tc_combine<MAGIC>(g, 2 * a), ls);
-      o.y = tc_unscale(tc_combine<MAGIC>(g, 2 * a + 1), ls);
-      tile[c ? pos[4 + a] : pos[a]] = o;
+      const long long yr = tc_shift(tc_combine<MAGIC>(g, 2 * a), lsl, lsr, rnd);
+      const long long yi = tc_shift(tc_combine<MAGIC>(g, 2 * a + 1), lsl, lsr, rnd);
+      tile[tc_pos(cbase | ((a & 1) ? d0 : 0) | ((a & 2) ? d1 : 0))] = make_longlong2(yr, yi);
     }
   }
 }
@@ -208,15 +209,14 @@ struct TcSync {
 // of column m: it gathers them, writes their digits (K columns 16h .. 16h+15
 // of row m) and, from TMEM lane m, their 16 outputs. The threads publish
 // each digit by arriving on s_afull; thread 0 waits there and issues that
-// digit's MMAs, so the other threads never wait for each other until the
-// epilogue.
+// digit's MMAs.
+template <bool MAGIC>
 __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, const TcPassParams& p, int basem,
                                          unsigned char* adig0, unsigned char* adig1, unsigned char* ubuf,
                                          uint32_t tbase, uint32_t tlane, uint64_t* s_afull, uint64_t* s_afree,
                                          uint64_t* s_acc, uint64_t* s_ufull, unsigned long long* s_cmax, TcSync& sy) {
   const int tid = threadIdx.x, h = tid >> 7, m = tid & 127;
   const uint32_t limit = p.wait_limit;
-  const int d[5] = {1 << st.bits[0], 1 << st.bits[1], 1 << st.bits[2], 1 << st.bits[3], 1 << st.bits[4]};
   if (st.u_index != sy.u_issued) {  // the first block of this CTA (later ones are prefetched)
     if (tid == 0) {
       mbar_arrive_expect_tx(s_ufull, kTcUBytes);
@@ -226,27 +226,31 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, con
     ++sy.n_u;
     sy.u_ready = false;
   }
-  // gather block rows 8h .. 8h+7 of column m; the column's scale (the bit
-  // length of its largest one's-complement magnitude)
-  int pos[8];
+  // gather block rows 8h .. 8h+7 of column m (block-row bits 3, 4 come from h);
+  // the column's scale from the bit length of its largest one's-complement magnitude
+  const int d0 = 1 << st.bits[0], d1 = 1 << st.bits[1], d2 = 1 << st.bits[2];
+  const int hbase = basem | ((h & 1) ? 1 << st.bits[3] : 0) | ((h & 2) ? 1 << st.bits[4] : 0);
   longlong2 v[8];
   unsigned long long mx = 0;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    pos[j] = tc_pos(basem | tc_dep(8 * h + j, d));
-    v[j] = tile[pos[j]];
+    v[j] = tile[tc_pos(hbase | ((j & 1) ? d0 : 0) | ((j & 2) ? d1 : 0) | ((j & 4) ? d2 : 0))];
     mx |= (unsigned long long)(v[j].x ^ (v[j].x >> 63)) | (unsigned long long)(v[j].y ^ (v[j].y >> 63));
   }
   s_cmax[tid] = mx;
   __syncthreads();
   mx = s_cmax[m] | s_cmax[m + 128] | s_cmax[m + 256] | s_cmax[m + 384];
-  const int bl = mx ? 64 - __clzll((long long)mx) : 0;
-  const int ls = mx ? 54 - bl : 0;
-  constexpr unsigned long long kBias = 0x0080808080808080ull;
+  const int bl = mx ? 64 - __clzll((long long)mx) : 54;
+  const int ls = 54 - bl;  // column scale 2^ls
+  {
+    const int lsl = ls > 0 ? ls : 0, lsr = ls < 0 ? -ls : 0;
+    const long long rnd = lsr ? (1ll << (lsr - 1)) : 0;
+    constexpr unsigned long long kBias = 0x0080808080808080ull;
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    v[j].x = (long long)((unsigned long long)tc_scale(v[j].x, ls) + kBias);
-    v[j].y = (long long)((unsigned long long)tc_scale(v[j].y, ls) + kBias);
+    for (int j = 0; j < 8; ++j) {
+      v[j].x = (long long)((unsigned long long)tc_shift(v[j].x, lsl, lsr, rnd) + kBias);
+      v[j].y = (long long)((unsigned long long)tc_shift(v[j].y, lsl, lsr, rnd) + kBias);
+    }
   }
   const uint32_t u_addr = (uint32_t)__cvta_generic_to_shared(ubuf);
   bool ok = true;
@@ -300,8 +304,7 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, con
     ++sy.n_u;
     sy.u_ready = false;
   }
-  if (st.magic) tc_epilogue<true>(tile, pos, h, ls, tlane);
-  else tc_epilogue<false>(tile, pos, h, ls, tlane);
+  tc_epilogue<MAGIC>(tile, hbase, d0, d1, d2, h, ls, tlane);
   tc_fence_before_sync();
   __syncthreads();
   return true;
@@ -319,6 +322,7 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
   __shared__ int s_red[kTcThreads / 32];
   __shared__ int s_high[16];
   __shared__ unsigned long long s_cmax[kTcThreads];
+  __shared__ TcStage s_stages[kTcSmemStages];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* const adig0 = base + 2 * kTcTileBytes;
@@ -326,6 +330,12 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
   unsigned char* ubuf = base + 2 * kTcTileBytes + 2 * kTcDigitBytes;
   const int tid = (int)threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid < 16) s_high[tid] = p.high[tid];
+  const TcStage* stages = p.stages;
+  if (p.num_stages <= kTcSmemStages) {
+    for (int i = tid; i < p.num_stages * (int)(sizeof(TcStage) / 4); i += kTcThreads)
+      reinterpret_cast<int*>(s_stages)[i] = reinterpret_cast<const int*>(p.stages)[i];
+    stages = s_stages;
+  }
   if (warp == 0) tc_alloc(&s_tbase, 512);
   if (tid == 0) {
     mbar_init(&s_full[0], 1);
@@ -408,7 +418,7 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
     }
     const int64_t tile_base = geom.base(tix);
     for (int si = 0; si < p.num_stages; ++si) {
-      const TcStage st = p.stages[si];
+      const TcStage st = stages[si];
       if (st.kind == TC_SWAP) {
         if (st.gctrl >= 0 && !((tile_base >> st.gctrl) & 1)) continue;
         const int tb = st.bits[0], cb = st.bits[1];
@@ -436,18 +446,16 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
         __syncthreads();
         continue;
       }
-      // dense block: the 7 tile bits outside it index the 128 columns
-      const uint32_t bmask = (1u << st.bits[0]) | (1u << st.bits[1]) | (1u << st.bits[2]) | (1u << st.bits[3]) |
-                             (1u << st.bits[4]);
+      // dense block: the 7 tile bits outside it (st.cols, 4 bits each) index the 128 columns
       const int m = tid & 127;
       int basem = 0;
-      for (int b = 0, c = 0; b < 12; ++b)
-        if (!(bmask & (1u << b))) {
-          basem |= ((m >> c) & 1) << b;
-          ++c;
-        }
-      if (!tc_block(tile, st, p, basem, adig0, adig1, ubuf, tbase, tlane, s_afull, s_afree, &s_acc, &s_ufull, s_cmax,
-                    sy)) {
+#pragma unroll
+      for (int c = 0; c < 7; ++c) basem |= ((m >> c) & 1) << ((st.cols >> (4 * c)) & 15);
+      const bool okb = st.magic ? tc_block<true>(tile, st, p, basem, adig0, adig1, ubuf, tbase, tlane, s_afull,
+                                                 s_afree, &s_acc, &s_ufull, s_cmax, sy)
+                                : tc_block<false>(tile, st, p, basem, adig0, adig1, ubuf, tbase, tlane, s_afull,
+                                                  s_afree, &s_acc, &s_ufull, s_cmax, sy);
+      if (!okb) {
         failed = true;
         break;
       }
