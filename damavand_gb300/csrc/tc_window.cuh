@@ -207,9 +207,9 @@ struct TcSync {
 // One dense block on the tile. Returns false if a wait gave up (uniform over
 // the CTA). Thread (h, m) = (tid / 128, tid % 128) owns block rows 8h .. 8h+7
 // of column m: it gathers them, writes their digits (K columns 16h .. 16h+15
-// of row m) and, from TMEM lane m, their 16 outputs. The threads publish
-// each digit by arriving on s_afull; thread 0 waits there and issues that
-// digit's MMAs.
+// of row m) and, from TMEM lane m, their 16 outputs. Each warp publishes a
+// digit by one arrival on s_afull once its lanes' stores are fenced and the
+// warp has synchronised; thread 0 waits there and issues that digit's MMAs.
 template <bool MAGIC>
 __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, const TcPassParams& p, int basem,
                                          unsigned char* adig0, unsigned char* adig1, unsigned char* ubuf,
@@ -272,7 +272,8 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, con
       if (ok) *reinterpret_cast<uint4*>(row + (size_t)c * 128) = w;
     }
     fence_proxy_async_smem();
-    mbar_arrive(&s_afull[ab]);
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(&s_afull[ab]);  // one arrival per warp
     if (tid == 0) {
       // the issuing thread polls (a suspended wait would delay the MMAs)
       bool go = ok && mbar_wait(&s_afull[ab], k & 1u, limit);
@@ -340,8 +341,8 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
   if (tid == 0) {
     mbar_init(&s_full[0], 1);
     mbar_init(&s_full[1], 1);
-    mbar_init(&s_afull[0], kTcThreads);
-    mbar_init(&s_afull[1], kTcThreads);
+    mbar_init(&s_afull[0], kTcThreads / 32);
+    mbar_init(&s_afull[1], kTcThreads / 32);
     mbar_init(&s_afree[0], 1);
     mbar_init(&s_afree[1], 1);
     mbar_init(&s_acc, 1);

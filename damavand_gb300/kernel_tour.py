@@ -4,7 +4,7 @@
 
 On an n-qubit complex128 state (and a complex64 copy) it launches, in order:
 the single-op pass (general, controlled), the window pass (FP64, FP32-pair,
-int64, complex64), the probability kernel, the Pauli-Z / chunk-mass reduction, the
+int64, tensor-core digit products, complex64), the probability kernel, the Pauli-Z / chunk-mass reduction, the
 sampler, the inner product, the observable scaling and the adjoint step (one
 small adjoint), the layout conversions of a host copy, the allocation-free
 expectation, and one batched persistent launch. Each prints its wall time so
@@ -19,7 +19,7 @@ import time
 import numpy as np
 
 from . import Circuit
-from ._lib import ARITH_FP32X2, ARITH_FP64, ARITH_INT64, C64, check, dptr, lib
+from ._lib import ARITH_FP32X2, ARITH_FP64, ARITH_INT64, ARITH_TC, C64, check, dptr, lib
 from .batch import Batch
 from .workloads import gate_array, ladder_circuit, loss_weights, ring_ansatz, uneven_batch
 
@@ -54,6 +54,7 @@ def main():
     _timed("window passes (fp64)", lambda: apply(1))
     _timed("window passes (fp32x2)", lambda: apply(1, ARITH_FP32X2))
     _timed("window passes (int64)", lambda: apply(1, ARITH_INT64))
+    _timed("window passes (tc)", lambda: apply(1, ARITH_TC))
     c64 = Circuit(n, precision="complex64")
     _timed("window passes (complex64)", lambda: apply(1, ARITH_FP64, c64.state()))
     probs = np.empty(1 << n) if n <= 28 else None
