@@ -203,17 +203,22 @@ constexpr int kTcURows = 64 * kTcDigits;                    // rows of a block's
 constexpr int64_t kTcUHalves = (int64_t)kTcURows * 64;      // FP16 elements per block (56 KB)
 enum TcStageKind : int32_t { TC_BLOCK = 0, TC_SWAP = 1 };
 
+// Exchanges are not applied to the data: the tile stays where it is and the
+// kernel reads logical amplitude l at phys(l) = A l xor c, an affine map over
+// the 12 tile bits. A CNOT with a control inside the tile changes A (the host
+// tracks it), X and CNOTs controlled from outside the tile change c (the
+// kernel, per tile).
 struct TcStage {
-  int32_t kind;     // TcStageKind
-  int32_t bits[5];  // block: tile bits of block-row bits 0..4 (ascending); swap: [0] target, [1] local control or -1
-  int32_t gctrl;    // swap: control qubit outside the tile, or -1
-  int32_t u_index;  // block: index of its digit matrix in the plan's array
-  int32_t magic;    // block: 1 when every FP32 accumulator stays below 2^22 in magnitude
-  int32_t next_u;   // block: u_index of the pass's next block (cyclically), fetched during this one's epilogue
-  int32_t cols;     // block: the 7 other tile bits (column index bits 0..6), 4 bits each
-  int32_t pad;
+  int32_t kind;       // TcStageKind
+  int32_t img[12];    // block: A e_b for the block's 5 bits (img[0..4], block-row bits 0..4) and its 7
+                      // other tile bits (img[5..11], column-index bits 0..6); swap: img[0] = mask xored into c
+  int32_t gctrl;      // swap: control qubit outside the tile (c changes on tiles where it is 1), or -1
+  int32_t u_index;    // block: index of its digit matrix in the plan's array
+  int32_t magic;      // block: 1 when every FP32 accumulator stays below 2^22 in magnitude
+  int32_t next_u;     // block: u_index of the pass's next block (cyclically), fetched during this one's epilogue
+  int32_t pad[3];
 };
-static_assert(sizeof(TcStage) == 48, "TcStage layout");
+static_assert(sizeof(TcStage) == 80, "TcStage layout");
 
 // Cuts window pass `ps` of `plan` (a 2^12-amplitude tile) into stages,
 // appended to `stages`, and appends each block's digit matrix (kTcUHalves
@@ -221,7 +226,10 @@ static_assert(sizeof(TcStage) == 48, "TcStage layout");
 // false, appending nothing, when the pass holds an op the tensor-core kernel
 // does not take (a non-unitary op, or a non-exchange op controlled from
 // outside the tile).
-bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stages, std::vector<uint16_t>& u);
+// `final_map` receives A e_b (b = 0..11) after the pass's last stage and
+// `exchanges` the number of X / CNOT ops applied as relabellings.
+bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stages, std::vector<uint16_t>& u,
+                   int32_t final_map[12], int32_t* exchanges);
 // Test hook (dmv_debug_tc_convert): 1 forces the exact conversion in every block.
 void set_tc_convert_mode(int32_t mode);
 

@@ -685,6 +685,8 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   std::vector<int64_t> tc_first(passes.size(), -1);
   std::vector<int32_t> tc_count(passes.size(), 0);
   std::vector<int32_t> tc_blocks(passes.size(), 0);
+  std::vector<int32_t> tc_maps(passes.size() * 12, 0);
+  std::vector<int32_t> tc_exchanges(passes.size(), 0);
   if (tc) {
     s->tc_stages.clear();
     s->tc_u.clear();
@@ -693,7 +695,7 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
       if (ps.kind != 1 || !tma_eligible<PolF64>(ps)) continue;
       const size_t mark = s->tc_stages.size();
       const size_t umark = s->tc_u.size();
-      if (!build_tc_pass(plan, ps, s->tc_stages, s->tc_u)) continue;
+      if (!build_tc_pass(plan, ps, s->tc_stages, s->tc_u, &tc_maps[i * 12], &tc_exchanges[i])) continue;
       tc_first[i] = (int64_t)mark;
       tc_count[i] = (int32_t)(s->tc_stages.size() - mark);
       tc_blocks[i] = (int32_t)((s->tc_u.size() - umark) / (size_t)kTcUHalves);
@@ -720,7 +722,7 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
       const int64_t tok = prof_begin(DMV_KERNEL_WINDOW, s->stream, (double)(2 * S), flops);
       DMV_TRY(launch_window_tc(s->amps, s->n, ps,
                                static_cast<const TcStage*>(s->tc_stages_dev.ptr) + tc_first[pi], tc_count[pi],
-                               static_cast<const uint16_t*>(s->tc_u_dev.ptr), s->stream));
+                               static_cast<const uint16_t*>(s->tc_u_dev.ptr), &tc_maps[pi * 12], s->stream));
       prof_end(tok, s->stream);
       bytes += 2 * S;
       count_launch();
@@ -765,7 +767,7 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     if (tc && tc_first[pi] >= 0) {
       ++s->last_tc_passes;
       s->last_tc_blocks += tc_blocks[pi];
-      s->last_tc_swaps += tc_count[pi] - tc_blocks[pi];
+      s->last_tc_swaps += tc_exchanges[pi];
     }
   s->last_passes = (int64_t)passes.size();
   s->last_ops = (int64_t)plan.ops.size();

@@ -6,9 +6,11 @@
 // dense block of at most 5 tile bits and takes, in order, every op whose bits
 // fit and none of whose bits an earlier op of the sweep left behind. An
 // exchange (X, CNOT) that touches no bit of the open block and none left
-// behind commutes with everything taken so far and becomes its own stage in
-// front of the block (an integer swap costs no arithmetic). The block's
-// matrix is the product of its ops, in order, as one 32 x 32 complex matrix.
+// behind commutes with everything taken so far and takes effect in front of
+// the block, as a relabelling: the kernel reads logical amplitude l at
+// A l xor c, A tracked here (CNOTs controlled inside the tile), c in the
+// kernel (X and CNOTs controlled outside it). The block's matrix is the
+// product of its ops, in order, as one 32 x 32 complex matrix.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -82,7 +84,8 @@ bool append_block_digits(const double* ur, const double* ui, std::vector<uint16_
 
 }  // namespace
 
-bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stages, std::vector<uint16_t>& u) {
+bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stages, std::vector<uint16_t>& u,
+                   int32_t final_map[12], int32_t* exchanges) {
   const int32_t k = ps.low_bits + ps.num_high;
   if (k != 12) return false;
   const Op* ops = plan.ops.data() + ps.op_begin;
@@ -92,6 +95,10 @@ bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stage
     if (ops[i].ctrl_kind == CTRL_GLOBAL && ops[i].cls != OP_SWAP) return false;
   }
   const size_t first_stage = stages.size();
+  // the affine map's linear part: amap[b] = A e_b
+  int32_t amap[12];
+  for (int b = 0; b < 12; ++b) amap[b] = 1 << b;
+  int32_t nx = 0;
   std::vector<int64_t> rem(count), keep, take;
   for (int64_t i = 0; i < count; ++i) rem[i] = i;
   std::vector<double> ur(32 * 32), ui(32 * 32);
@@ -109,15 +116,19 @@ bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stage
         continue;
       }
       if (op.cls == OP_SWAP && !(qs & S)) {
-        TcStage st;
-        std::memset(&st, 0, sizeof(st));
-        st.kind = TC_SWAP;
-        st.bits[0] = op.target;
-        st.bits[1] = op.ctrl_kind == CTRL_LOCAL ? op.ctrl : -1;
-        st.gctrl = op.ctrl_kind == CTRL_GLOBAL ? op.ctrl : -1;
-        for (int b = 2; b < 5; ++b) st.bits[b] = -1;
-        st.u_index = -1;
-        stages.push_back(st);
+        // new phys(l) = old phys(sigma(l)), sigma the exchange on logical indices
+        ++nx;
+        if (op.ctrl_kind == CTRL_LOCAL) {
+          amap[op.ctrl] ^= amap[op.target];  // sigma(l) = l xor l_ctrl e_target: linear
+        } else {
+          TcStage st;  // sigma(l) = l xor e_target (on the tiles where the control is 1): c ^= A e_target
+          std::memset(&st, 0, sizeof(st));
+          st.kind = TC_SWAP;
+          st.img[0] = amap[op.target];
+          st.gctrl = op.ctrl_kind == CTRL_GLOBAL ? op.ctrl : -1;
+          st.u_index = -1;
+          stages.push_back(st);
+        }
         continue;
       }
       if (op.ctrl_kind == CTRL_GLOBAL) {  // an exchange overlapping the open block: a later sweep
@@ -168,9 +179,9 @@ bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stage
       TcStage st;
       std::memset(&st, 0, sizeof(st));
       st.kind = TC_BLOCK;
-      for (int b = 0; b < kTcBlockBits; ++b) st.bits[b] = bits[b];
+      for (int b = 0; b < kTcBlockBits; ++b) st.img[b] = amap[bits[b]];
       for (int b = 0, c = 0; b < k; ++b)
-        if (!(S & (1u << b))) st.cols |= b << (4 * c++);
+        if (!(S & (1u << b))) st.img[kTcBlockBits + c++] = amap[b];
       st.gctrl = -1;
       st.u_index = (int32_t)(u.size() / (size_t)kTcUHalves);
       st.magic = append_block_digits(ur.data(), ui.data(), u) && g_tc_convert_mode == 0 ? 1 : 0;
@@ -184,6 +195,8 @@ bool build_tc_pass(const Plan& plan, const Pass& ps, std::vector<TcStage>& stage
     if (stages[i].kind == TC_BLOCK) blocks.push_back(i);
   for (size_t b = 0; b < blocks.size(); ++b)
     stages[blocks[b]].next_u = stages[blocks[(b + 1) % blocks.size()]].u_index;
+  for (int b = 0; b < 12; ++b) final_map[b] = amap[b];
+  if (exchanges) *exchanges = nx;
   return true;
 }
 

@@ -10,7 +10,9 @@
 //     (56 fraction bits, tc_from_double). Amplitude l sits at
 //     l ^ ((l >> 5) & 7), which keeps the column gathers below free of
 //     bank conflicts.
-//  2. Exchange stages swap amplitude pairs in shared memory.
+//  2. Exchanges move no data: logical amplitude l of the tile is read at
+//     A l xor c, A given by the host per block (CNOTs controlled inside the
+//     tile), c updated per tile here (X, and CNOTs controlled outside it).
 //  3. A block stage views the tile as 128 columns x 32 block rows. Threads
 //     t, t + 128, t + 256, t + 384 gather quarters of column t, scale it so its largest
 //     component is below 2^54, and write its 7 balanced 8-bit digits (FP16)
@@ -47,6 +49,7 @@ struct TcPassParams {
   int32_t num_stages;
   const TcStage* stages;
   const uint16_t* u;
+  int32_t final_map[12];  // A e_b after the pass's last stage (the linear part of the final relabelling)
 };
 
 // Tile fixed point: with e the tile's largest biased FP64 exponent, x becomes
@@ -168,12 +171,12 @@ __device__ __forceinline__ void tc_epilogue(longlong2* tile, int hbase, int d0, 
 #pragma unroll
     for (int s = 0; s < 8; ++s) tc_ld8(tlane + (uint32_t)(64 * s + 8 * q), g[s]);
     tc_wait_ld();
-    const int cbase = hbase | (c ? d2 : 0);
+    const int cbase = hbase ^ (c ? d2 : 0);
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       const long long yr = tc_shift(tc_combine<MAGIC>(g, 2 * a), lsl, lsr, rnd);
       const long long yi = tc_shift(tc_combine<MAGIC>(g, 2 * a + 1), lsl, lsr, rnd);
-      tile[tc_pos(cbase | ((a & 1) ? d0 : 0) | ((a & 2) ? d1 : 0))] = make_longlong2(yr, yi);
+      tile[tc_pos(cbase ^ ((a & 1) ? d0 : 0) ^ ((a & 2) ? d1 : 0))] = make_longlong2(yr, yi);
     }
   }
 }
@@ -226,15 +229,16 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, con
     ++sy.n_u;
     sy.u_ready = false;
   }
-  // gather block rows 8h .. 8h+7 of column m (block-row bits 3, 4 come from h);
-  // the column's scale from the bit length of its largest one's-complement magnitude
-  const int d0 = 1 << st.bits[0], d1 = 1 << st.bits[1], d2 = 1 << st.bits[2];
-  const int hbase = basem | ((h & 1) ? 1 << st.bits[3] : 0) | ((h & 2) ? 1 << st.bits[4] : 0);
+  // gather block rows 8h .. 8h+7 of column m (block-row bits 3, 4 come from h)
+  // through the tile's relabelling (basem already holds A m xor c); the
+  // column's scale from the bit length of its largest one's-complement magnitude
+  const int d0 = st.img[0], d1 = st.img[1], d2 = st.img[2];
+  const int hbase = basem ^ ((h & 1) ? st.img[3] : 0) ^ ((h & 2) ? st.img[4] : 0);
   longlong2 v[8];
   unsigned long long mx = 0;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    v[j] = tile[tc_pos(hbase | ((j & 1) ? d0 : 0) | ((j & 2) ? d1 : 0) | ((j & 4) ? d2 : 0))];
+    v[j] = tile[tc_pos(hbase ^ ((j & 1) ? d0 : 0) ^ ((j & 2) ? d1 : 0) ^ ((j & 4) ? d2 : 0))];
     mx |= (unsigned long long)(v[j].x ^ (v[j].x >> 63)) | (unsigned long long)(v[j].y ^ (v[j].y >> 63));
   }
   s_cmax[tid] = mx;
@@ -418,40 +422,18 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
       }
     }
     const int64_t tile_base = geom.base(tix);
+    int cst = 0;  // the affine part c of the tile's relabelling
     for (int si = 0; si < p.num_stages; ++si) {
-      const TcStage st = stages[si];
+      const TcStage& st = stages[si];
       if (st.kind == TC_SWAP) {
-        if (st.gctrl >= 0 && !((tile_base >> st.gctrl) & 1)) continue;
-        const int tb = st.bits[0], cb = st.bits[1];
-        if (cb < 0) {
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int l0 = tc_insert_zero(tid + kTcThreads * j, tb), l1 = l0 | (1 << tb);
-            const int p0 = tc_pos(l0), p1 = tc_pos(l1);
-            const longlong2 a0 = tile[p0], a1 = tile[p1];
-            tile[p0] = a1;
-            tile[p1] = a0;
-          }
-        } else {
-          const int lo = min(tb, cb), hi = max(tb, cb);
-#pragma unroll
-          for (int j = 0; j < 2; ++j) {
-            const int l0 = tc_insert_zero(tc_insert_zero(tid + kTcThreads * j, lo), hi) | (1 << cb);
-            const int l1 = l0 | (1 << tb);
-            const int p0 = tc_pos(l0), p1 = tc_pos(l1);
-            const longlong2 a0 = tile[p0], a1 = tile[p1];
-            tile[p0] = a1;
-            tile[p1] = a0;
-          }
-        }
-        __syncthreads();
+        if (st.gctrl < 0 || ((tile_base >> st.gctrl) & 1)) cst ^= st.img[0];
         continue;
       }
-      // dense block: the 7 tile bits outside it (st.cols, 4 bits each) index the 128 columns
+      // dense block: the 7 tile bits outside it (images img[5..11]) index the 128 columns
       const int m = tid & 127;
-      int basem = 0;
+      int basem = cst;
 #pragma unroll
-      for (int c = 0; c < 7; ++c) basem |= ((m >> c) & 1) << ((st.cols >> (4 * c)) & 15);
+      for (int c = 0; c < 7; ++c) basem ^= ((m >> c) & 1) ? st.img[kTcBlockBits + c] : 0;
       const bool okb = st.magic ? tc_block<true>(tile, st, p, basem, adig0, adig1, ubuf, tbase, tlane, s_afull,
                                                  s_afree, &s_acc, &s_ufull, s_cmax, sy)
                                 : tc_block<false>(tile, st, p, basem, adig0, adig1, ubuf, tbase, tlane, s_afull,
@@ -463,9 +445,14 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
     }
     if (failed) break;
     // int64 -> FP64, back to the linear layout, out by TMA
+    // logical amplitude tid + 512 j sits at A (tid + 512 j) xor c
+    int atid = cst;
+#pragma unroll
+    for (int b = 0; b < 9; ++b) atid ^= ((tid >> b) & 1) ? p.final_map[b] : 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const longlong2 x = tile[tc_pos(tid + kTcThreads * j)];
+      const int aj = ((j & 1) ? p.final_map[9] : 0) ^ ((j & 2) ? p.final_map[10] : 0) ^ ((j & 4) ? p.final_map[11] : 0);
+      const longlong2 x = tile[tc_pos(atid ^ aj)];
       dd[j] = make_double2(fx_to_double(x.x, e - 2), fx_to_double(x.y, e - 2));  // X * 2^(e - 1078)
     }
     __syncthreads();
@@ -499,7 +486,7 @@ k_window_tc(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ Tc
 }
 
 int launch_window_tc(void* amps, int32_t n, const Pass& ps, const TcStage* stages_dev, int32_t num_stages,
-                     const uint16_t* u_dev, cudaStream_t stream) {
+                     const uint16_t* u_dev, const int32_t final_map[12], cudaStream_t stream) {
   if ((reinterpret_cast<uintptr_t>(amps) & 15u) != 0)
     return set_error(DMV_ERR_INVALID, "statevector not 16-byte aligned");
   CUtensorMap map;
@@ -518,6 +505,7 @@ int launch_window_tc(void* amps, int32_t n, const Pass& ps, const TcStage* stage
   p.num_stages = num_stages;
   p.stages = stages_dev;
   p.u = u_dev;
+  for (int b = 0; b < 12; ++b) p.final_map[b] = final_map[b];
   static bool configured = false;
   if (!configured) {
     DMV_CUDA_TRY(cudaFuncSetAttribute(k_window_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
