@@ -57,6 +57,17 @@ __device__ __forceinline__ void tc_mma_f16(uint32_t d_tmem, uint64_t a_desc, uin
       : "memory");
 }
 
+// True in exactly one lane of the (fully active) warp: the lowest.
+__device__ __forceinline__ bool tc_elect_one() {
+  uint32_t e;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "elect.sync _|p, 0xffffffff;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(e));
+  return e != 0;
+}
+
 // Arrives (once) on `bar` when every tcgen05 operation this thread issued
 // before has completed.
 __device__ __forceinline__ void tc_commit(uint64_t* bar) {

@@ -117,7 +117,12 @@ __device__ __forceinline__ unsigned tc_acc_biased(uint32_t bits) {
   else return (unsigned)(__float2int_rn(__uint_as_float(bits)) + kTcMagic);
 }
 
-__device__ __forceinline__ void tc_issue_digit(int digit, uint32_t tbase, uint32_t a_addr, uint32_t u_addr) {
+// Called by a whole warp (the descriptors are warp-uniform); the elected lane
+// issues. A descriptor's address field is its low 14 bits (shared-memory byte
+// address / 16, below 2^14 for addresses under 256 KB), so an offset is added
+// to a base descriptor as offset / 16.
+__device__ __forceinline__ void tc_issue_digit(int digit, uint32_t tbase, uint64_t a_desc, uint64_t u_desc,
+                                               bool leader) {
 #pragma unroll
   for (int e = 0; e < 12; ++e) {
     const TcMma m = kTcMmas[e];
@@ -125,9 +130,9 @@ __device__ __forceinline__ void tc_issue_digit(int digit, uint32_t tbase, uint32
     const uint32_t idesc = tc_idesc_f16(128, m.n);
 #pragma unroll
     for (int ks = 0; ks < 4; ++ks) {
-      const uint64_t ad = tc_smem_desc(a_addr + (uint32_t)ks * 256u, 128, 1024);
-      const uint64_t bd = tc_smem_desc(u_addr + (uint32_t)(m.row0 >> 3) * 1024u + (uint32_t)ks * 256u, 128, 1024);
-      tc_mma_f16(tbase + (uint32_t)m.col0, ad, bd, idesc, m.init ? (uint32_t)(ks > 0) : 1u);
+      const uint64_t ad = a_desc + (uint64_t)(ks * 16);
+      const uint64_t bd = u_desc + (uint64_t)((m.row0 >> 3) * 64 + ks * 16);
+      if (leader) tc_mma_f16(tbase + (uint32_t)m.col0, ad, bd, idesc, m.init ? (uint32_t)(ks > 0) : 1u);
     }
   }
 }
@@ -256,7 +261,7 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, con
       v[j].y = (long long)((unsigned long long)tc_shift(v[j].y, lsl, lsr, rnd) + kBias);
     }
   }
-  const uint32_t u_addr = (uint32_t)__cvta_generic_to_shared(ubuf);
+  const uint64_t u_desc = tc_smem_desc((uint32_t)__cvta_generic_to_shared(ubuf), 128, 1024);
   bool ok = true;
 #pragma unroll
   for (int i = 0; i < kTcDigits; ++i) {
@@ -278,18 +283,23 @@ __device__ __forceinline__ bool tc_block(longlong2* tile, const TcStage& st, con
     fence_proxy_async_smem();
     __syncwarp();
     if ((tid & 31) == 0) mbar_arrive(&s_afull[ab]);  // one arrival per warp
-    if (tid == 0) {
-      // the issuing thread polls (a suspended wait would delay the MMAs)
+    if (tid < 32) {
+      // warp 0 polls (a suspended wait would delay the MMAs) and one lane issues
       bool go = ok && mbar_wait(&s_afull[ab], k & 1u, limit);
       if (i == 0 && !sy.u_ready) go = go && mbar_wait(s_ufull, (sy.n_u - 1) & 1u, limit);
+      go = __all_sync(0xffffffffu, go);
+      const bool leader = tc_elect_one();
       if (go) {
         tc_fence_after_sync();
-        tc_issue_digit(i, tbase, (uint32_t)__cvta_generic_to_shared(abuf), u_addr);
+        tc_issue_digit(i, tbase, tc_smem_desc((uint32_t)__cvta_generic_to_shared(abuf), 128, 1024), u_desc, leader);
       }
       ok = go;
       // commits arrive even after a failure, so no thread waits on them forever
-      tc_commit(&s_afree[ab]);
-      if (i == kTcDigits - 1) tc_commit(s_acc);
+      if (leader) {
+        tc_commit(&s_afree[ab]);
+        if (i == kTcDigits - 1) tc_commit(s_acc);
+      }
+      __syncwarp();
     }
     if (ab) ++sy.n_afree1;
     else ++sy.n_afree0;
