@@ -14,7 +14,9 @@ def main():
     bench.barrier(world)
     mine = 10.0 * (rank + 1)
     top = bench.max_over_ranks(world, mine)
-    print(json.dumps({"rank": rank, "local": local, "world": world, "mine": mine, "max": top}), flush=True)
+    # one write() per line: both ranks share the pipe, and a write under PIPE_BUF is atomic
+    line = json.dumps({"rank": rank, "local": local, "world": world, "mine": mine, "max": top}) + "\n"
+    os.write(1, line.encode())
     import torch.distributed as dist
     dist.destroy_process_group()
 

@@ -175,3 +175,49 @@ def test_tc_adjoint_gradient(built_lib, oracle_mod):
     ps = oracle_mod.param_shift_grad(n, gates, parameters(gates), w)
     assert abs(loss - oracle_mod.loss(n, gates, parameters(gates), w)) < 1e-12
     assert np.max(np.abs(g - ps)) < 1e-10
+
+
+def test_tc_non_unitary_matrix_falls_back(built_lib, oracle_mod):
+    """A pass holding a non-unitary explicit matrix runs in FP64 (the digit
+    bounds rely on unitary blocks); the other passes still use the tensor cores."""
+    from damavand_gb300._lib import Gate, check, lib
+    from damavand_gb300.workloads import ladder_circuit
+    n = 14
+    rng = np.random.default_rng(23)
+    psi = random_state(n, rng)
+    tail = [g for g in ladder_circuit(n, 2, seed=9) if not g[3]]
+    st = _state(n)
+    try:
+        load_state(st, psi)
+        g = (Gate * (2 + len(tail)))()
+        g[0].kind, g[0].target, g[0].control = 8, 3, -1          # diag(2, 0.5): not unitary
+        g[0].m[0], g[0].m[6] = 2.0, 0.5
+        g[1].kind, g[1].target, g[1].control, g[1].theta = 4, 3, -1, 0.7
+        for i, (kind, t, c, _obs, th) in enumerate(tail):
+            g[2 + i].kind, g[2 + i].target, g[2 + i].control, g[2 + i].theta = kind, t, c, th
+        check(lib.dmv_apply_gates(st.handle, g, 2 + len(tail), 1))
+        want = psi.copy()
+        oracle_mod.apply_gate(want, n, np.array([[2.0, 0], [0, 0.5]]), -1, 3)
+        oracle_mod.forward(n, [(4, 3, -1, 0, 0.7)] + [(k, t, c, 0, th) for (k, t, c, _o, th) in tail], want)
+        assert_state_close(st.numpy(), want, rtol=1e-13, what="non-unitary pass")
+    finally:
+        free_state(st)
+
+
+@pytest.mark.parametrize("n,fusion", [(3, 1), (8, 1), (11, 1), (14, 0)])
+def test_tc_small_states_and_unfused_lists(built_lib, oracle_mod, n, fusion):
+    """States smaller than one 2^12-amplitude tile and unfused gate lists take the
+    integer-pipe kernels of the same arithmetic; results stay at oracle level."""
+    from damavand_gb300.workloads import random_circuit
+    rng = np.random.default_rng(300 + n)
+    gates = random_circuit(n, 8, rng)
+    psi = random_state(n, rng)
+    want = oracle_mod.forward(n, gates, psi.copy())
+    st = _state(n)
+    try:
+        load_state(st, psi)
+        apply_gates(st, gates, fusion)
+        assert _tc_stats(st)[0] == 0
+        assert_state_close(st.numpy(), want, rtol=1e-13, what=f"n={n} fusion={fusion}")
+    finally:
+        free_state(st)
