@@ -1,6 +1,6 @@
 """ctypes bindings of libdamavand_gpu.so (the C ABI in include/damavand_gpu.h).
 
-The library must have been built (``python -m damavand_gb300.build`` or
+The library must have been built (``python damavand_gb300/build.py`` or
 ``__graft_entry__.build()``); importing without it raises ImportError.
 There is no CPU fallback: every call runs on the GPU through the library.
 """
@@ -136,7 +136,7 @@ SIGNATURES = {
 def _load() -> ctypes.CDLL:
     if not os.path.exists(LIB_PATH):
         raise ImportError(
-            f"{LIB_PATH} is missing: build it with `python -m damavand_gb300.build` "
+            f"{LIB_PATH} is missing: build it with `python damavand_gb300/build.py` "
             "(the GPU library is required; there is no CPU fallback)")
     lib = ctypes.CDLL(LIB_PATH)
     for name, (res, args) in SIGNATURES.items():
