@@ -56,10 +56,10 @@ FP32_FMA_PEAK_T = 35.9
 # dram__bytes_read.sum + dram__bytes_write.sum per launch divided by the amplitudes of
 # the captured case (profiles/k_window_tma_fp64_24q_full.md: 479.9 MB at 2^24;
 # profiles/k_window_phases_c64_26q_full.md: 1012.3 MB at 2^26;
-# profiles/k_window_tc_24q_full.md: 475.3 MB at 2^24).
+# profiles/k_window_tc_24q_full.md: 476.1 MB at 2^24).
 NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 479.873280e6 / (1 << 24),
                              ("window", "c64"): 1012.291328e6 / (1 << 26),
-                             ("window", "c128", "tc"): 475.291648e6 / (1 << 24)}
+                             ("window", "c128", "tc"): 476.122112e6 / (1 << 24)}
 # The kernel that runs a fused window pass, by arithmetic and precision.
 WINDOW_KERNEL = {("fp64", "c128"): "k_window_tma<PolF64>", ("fp32x2", "c128"): "k_apply_window<PolDF>",
                  ("int64", "c128"): "k_apply_window<PolFX>", ("tc", "c128"): "k_window_tc",
