@@ -4,6 +4,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -961,9 +962,41 @@ namespace {
 std::mutex g_legacy_mu;
 dmv_state_t g_legacy = nullptr;
 int64_t g_n_apply = 0;
+// Gates applied through the per-gate legacy call are queued and run as one
+// fused gate list (qubit-window passes) when the state is next read, loaded
+// or when the queue is long: the reference front-end calls once per gate
+// (src/qubit_backend/circuit_gpu.rs:31-60), and every read of the state goes
+// through this library, so the deferral is invisible to it.
+std::vector<dmv_gate_t> g_legacy_pending;
+constexpr size_t kLegacyQueue = 8192;
 
 void legacy_report(const char* where) {
   std::fprintf(stderr, "damavand_gb300: %s: %s\n", where, g_last_msg);
+}
+
+// Runs the queued legacy gates (caller holds g_legacy_mu).
+void legacy_flush(const char* where) {
+  if (g_legacy_pending.empty() || !g_legacy) {
+    g_legacy_pending.clear();
+    return;
+  }
+  const int rc = dmv_apply_gates(g_legacy, g_legacy_pending.data(), (int64_t)g_legacy_pending.size(),
+                                 DMV_FUSE_WINDOW);
+  g_legacy_pending.clear();
+  if (rc != DMV_OK) legacy_report(where);
+}
+
+// Complex128 arithmetic of the legacy state: DAMAVAND_GB300_ARITHMETIC = fp64
+// (default), fp32x2, int64 or tc, so an unchanged front-end can select it.
+int32_t legacy_arithmetic() {
+  const char* v = std::getenv("DAMAVAND_GB300_ARITHMETIC");
+  if (!v || !*v) return DMV_ARITH_FP64;
+  const std::string a(v);
+  if (a == "fp32x2") return DMV_ARITH_FP32X2;
+  if (a == "int64") return DMV_ARITH_INT64;
+  if (a == "tc") return DMV_ARITH_TC;
+  if (a != "fp64") std::fprintf(stderr, "damavand_gb300: unknown DAMAVAND_GB300_ARITHMETIC '%s': fp64\n", v);
+  return DMV_ARITH_FP64;
 }
 
 int log2_exact(int64_t v) {
@@ -1013,6 +1046,8 @@ extern "C" int peer_access_allowed(int, int) { return 0; }
 
 extern "C" void print_timers(void) {
   // Kernel timings come from CUDA events and ncu; this prints call counts.
+  std::lock_guard<std::mutex> lk(g_legacy_mu);
+  legacy_flush("print_timers");
   std::printf("apply calls %lld\n", (long long)g_n_apply);
   std::printf("kernel launches %lld\n", (long long)dmv_kernel_launch_count());
 }
@@ -1031,6 +1066,7 @@ extern "C" void init_quantum_state(int num_amplitudes_per_gpu, int num_gpus_per_
     legacy_report("init_quantum_state");
     return;
   }
+  g_legacy_pending.clear();  // gates queued for the state being replaced
   if (g_legacy && g_legacy->n != n) {
     dmv_state_destroy(g_legacy);
     g_legacy = nullptr;
@@ -1041,6 +1077,7 @@ extern "C" void init_quantum_state(int num_amplitudes_per_gpu, int num_gpus_per_
       g_legacy = nullptr;
       return;
     }
+    dmv_state_set_arithmetic(g_legacy, legacy_arithmetic());
   }
   // |0...0> on the first node, the zero vector otherwise (rust_communication.cu:185-194).
   if (is_first_node) {
@@ -1062,9 +1099,29 @@ extern "C" void apply_one_qubit_gate_gpu_local(double* gate_matrix_real, double*
     legacy_report("apply_one_qubit_gate_gpu_local");
     return;
   }
-  if (dmv_apply_matrix(g_legacy, gate_matrix_real, gate_matrix_imaginary, control_qubit < 0 ? -1 : control_qubit,
-                       target_qubit) != DMV_OK)
+  if (!gate_matrix_real || !gate_matrix_imaginary) {
+    set_error(DMV_ERR_INVALID, "null matrix");
     legacy_report("apply_one_qubit_gate_gpu_local");
+    return;
+  }
+  const int control = control_qubit < 0 ? -1 : control_qubit;
+  if (target_qubit < 0 || target_qubit >= g_legacy->n || control >= g_legacy->n || control == target_qubit) {
+    set_error(DMV_ERR_INVALID, "bad qubits: target %d control %d for %d qubits", target_qubit, control_qubit,
+              g_legacy->n);
+    legacy_report("apply_one_qubit_gate_gpu_local");
+    return;
+  }
+  dmv_gate_t g;
+  std::memset(&g, 0, sizeof(g));
+  g.kind = DMV_GATE_MATRIX;
+  g.target = target_qubit;
+  g.control = control;
+  for (int k = 0; k < 4; ++k) {
+    g.m[2 * k] = gate_matrix_real[k];
+    g.m[2 * k + 1] = gate_matrix_imaginary[k];
+  }
+  g_legacy_pending.push_back(g);
+  if (g_legacy_pending.size() >= kLegacyQueue) legacy_flush("apply_one_qubit_gate_gpu_local");
   ++g_n_apply;
 }
 
@@ -1072,6 +1129,7 @@ extern "C" void measure_on_gpu(int num_amplitudes_per_gpu, double* probabilities
   std::lock_guard<std::mutex> lk(g_legacy_mu);
   clear_error();
   if (!legacy_ready("measure_on_gpu", num_amplitudes_per_gpu)) return;
+  legacy_flush("measure_on_gpu");
   if (dmv_measure(g_legacy, probabilities) != DMV_OK) legacy_report("measure_on_gpu");
 }
 
@@ -1088,6 +1146,7 @@ extern "C" void retrieve_amplitudes_on_host(int num_amplitudes_per_gpu, double* 
   std::lock_guard<std::mutex> lk(g_legacy_mu);
   clear_error();
   if (!legacy_ready("retrieve_amplitudes_on_host", num_amplitudes_per_gpu)) return;
+  legacy_flush("retrieve_amplitudes_on_host");
   if (dmv_state_copy_to_host(g_legacy, local_amplitudes_real, local_amplitudes_imaginary) != DMV_OK)
     legacy_report("retrieve_amplitudes_on_host");
 }
@@ -1097,6 +1156,7 @@ extern "C" void load_amplitudes_local_on_device(int num_amplitudes_per_gpu, doub
   std::lock_guard<std::mutex> lk(g_legacy_mu);
   clear_error();
   if (!legacy_ready("load_amplitudes_local_on_device", num_amplitudes_per_gpu)) return;
+  g_legacy_pending.clear();  // the load replaces every amplitude the queued gates would change
   if (dmv_state_load_from_host(g_legacy, local_amplitudes_real, local_amplitudes_imaginary) != DMV_OK)
     legacy_report("load_amplitudes_local_on_device");
 }

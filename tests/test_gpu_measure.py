@@ -228,3 +228,46 @@ def test_torch_view_zero_copy(built_lib):
     t = c.state().torch()
     assert t.is_cuda and t.dtype == torch.complex128 and t.numel() == 32
     assert abs(t[0].item() - 2 ** -0.5) < 1e-15 and abs(t[1].item() - 2 ** -0.5) < 1e-15
+
+
+@pytest.mark.parametrize("arith", ["fp64", "tc"])
+def test_legacy_per_gate_calls_run_fused(built_lib, oracle_mod, arith, monkeypatch):
+    """The reference front-end's call sequence (circuit_gpu.rs:31-60: one call per gate, each
+    with its row-major 2x2 split into real and imaginary parts) on a 14-qubit ladder: the
+    library queues the calls and runs them as fused passes when the state is read, in the
+    arithmetic DAMAVAND_GB300_ARITHMETIC names, with oracle-level results."""
+    import math
+
+    from damavand_gb300._lib import dptr, lib
+    from damavand_gb300.workloads import ladder_circuit
+    monkeypatch.setenv("DAMAVAND_GB300_ARITHMETIC", arith)
+    n = 14 if arith == "fp64" else 15  # a new size makes init create the state (and read the variable)
+    N = 1 << n
+    gates = [g for g in ladder_circuit(n, 3, seed=11) if not g[3]]
+    h = 1 / math.sqrt(2.0)
+
+    def matrix(kind, theta):
+        c, s = math.cos(theta / 2), math.sin(theta / 2)
+        return {0: np.array([[h, h], [h, -h]], dtype=complex), 1: np.array([[0, 1], [1, 0]], dtype=complex),
+                4: np.array([[c, -1j * s], [-1j * s, c]]), 5: np.array([[c, -s], [s, c]], dtype=complex),
+                6: np.array([[complex(math.cos(-theta / 2), math.sin(-theta / 2)), 0],
+                             [0, complex(math.cos(theta / 2), math.sin(theta / 2))]]),
+                7: np.array([[0, 1], [1, 0]], dtype=complex)}[kind]
+
+    lib.init_quantum_state(N, 1, 1)
+    assert lib.dmv_last_error() == 0
+    launches0 = lib.dmv_kernel_launch_count()
+    for kind, t, c, _obs, theta in gates:
+        m = matrix(kind, theta)
+        mre, mim = np.ascontiguousarray(m.real.reshape(-1)), np.ascontiguousarray(m.imag.reshape(-1))
+        lib.apply_one_qubit_gate_gpu_local(dptr(mre), dptr(mim), n, N, c, t)
+        assert lib.dmv_last_error() == 0
+    re, im = np.empty(N), np.empty(N)
+    lib.retrieve_amplitudes_on_host(N, dptr(re), dptr(im))
+    assert lib.dmv_last_error() == 0
+    assert lib.dmv_kernel_launch_count() - launches0 < len(gates) // 4
+    want = oracle_mod.forward(n, gates)
+    assert_state_close(re + 1j * im, want, rtol=1e-13, what=f"legacy {arith}")
+    probs = np.empty(N)
+    lib.measure_on_gpu(N, dptr(probs))
+    np.testing.assert_allclose(probs, np.abs(want) ** 2, atol=1e-14)
