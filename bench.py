@@ -542,8 +542,20 @@ def run_ours(args, world, rank, local):
     t_p = time.perf_counter() - t0
     del probs
     torch.cuda.empty_cache()
+    # sampled <Z_q> for every qubit from 2^20 samples drawn and counted on the device (seeded stream)
+    k_se = 1 << 20
+    qs = np.arange(n, dtype=np.int32)
+    se_means = np.empty(n)
+    qptr = qs.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    check(lib.dmv_sample_expect_z(st.handle, None, 5, 4096, qptr, n, dptr(se_means), None))
+    t0 = time.perf_counter()
+    check(lib.dmv_sample_expect_z(st.handle, None, 5, k_se, qptr, n, dptr(se_means), None))
+    t_se = time.perf_counter() - t0
+    se_sigma = np.sqrt(np.maximum(1.0 - ez ** 2, 1e-12) / k_se)
     out["readout"] = {"expect_z_ms": t_ez * 1e3, "expect_z_gbs": S / t_ez / 1e9, "sample_1000_ms": t_s * 1e3,
                       "probabilities_on_device_ms": t_p * 1e3, "probabilities_gbs": (S + S // 2) / t_p / 1e9,
+                      "sample_expect_z": {"samples": k_se, "ms": t_se * 1e3, "samples_per_s": k_se / t_se,
+                                          "max_dev_over_sigma_vs_exact": float(np.max(np.abs(se_means - ez) / se_sigma))},
                       "norm": float(c.norm()), "first_samples": [int(x) for x in samples[:4]],
                       "mean_abs_expect_z": float(np.mean(np.abs(ez)))}
 

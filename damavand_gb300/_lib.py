@@ -83,6 +83,7 @@ SIGNATURES = {
     "dmv_expect_z": (ctypes.c_int, [_vp, _dp, _dp]),
     "dmv_sample": (ctypes.c_int, [_vp, _dp, _i64, _u64p]),
     "dmv_sample_probabilities": (ctypes.c_int, [_dp, _i64, _dp, _i64, _u64p]),
+    "dmv_sample_expect_z": (ctypes.c_int, [_vp, _dp, ctypes.c_uint64, _i64, _i32p, _i32, _dp, _i64p]),
     "dmv_inner_product": (ctypes.c_int, [_vp, _vp, _dp, _dp]),
     "dmv_expect_z_noalloc": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp]),
     "dmv_adjoint_gradient": (ctypes.c_int, [_vp, ctypes.POINTER(Gate), _i64, _dp, _dp, _dp]),
@@ -112,6 +113,7 @@ SIGNATURES = {
     "dmv_circuit_state": (ctypes.c_int, [_vp, _vpp]),
     "dmv_circuit_observables": (ctypes.c_int, [_vp, _i32p]),
     "dmv_circuit_extract_expectation_values": (ctypes.c_int, [_vp, _u64p, _i64, _dp]),
+    "dmv_circuit_sample_expectation_values": (ctypes.c_int, [_vp, _dp, ctypes.c_uint64, _i64, _dp]),
     "dmv_circuit_fidelity_with_parameters": (ctypes.c_int, [_vp, _dp, _i64, _dp, _i64, _dp]),
     "dmv_circuit_adjoint": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     # legacy ABI (void / int / double returns, C int sizes)

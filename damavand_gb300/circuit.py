@@ -261,6 +261,30 @@ class Circuit:
         check(lib.dmv_circuit_extract_expectation_values(self._h, u64ptr(s), s.size, dptr(out)))
         return out[:, :nobs].tolist()
 
+    def sample_expectation_values(self, num_samples: int | None = None, *, uniforms=None,
+                                  seed: int | None = None) -> np.ndarray:
+        """Per observable, the mean over num_samples samples (default 1000) of
+        extract_expectation_values (circuit.rs:494-513), with sampling and
+        counting on the GPU: the samples never reach the host.
+
+        `uniforms` (num_samples values in [0,1)) gives the same samples as
+        sample(uniforms=...); otherwise they are drawn on the device from the
+        SplitMix64 stream of `seed` (a random seed when None).
+        """
+        if uniforms is not None:
+            u = np.ascontiguousarray(np.asarray(uniforms, dtype=np.float64).reshape(-1))
+            if num_samples is not None and u.size != int(num_samples):
+                raise ValueError(f"{u.size} uniforms given for {num_samples} samples")
+            k, up, sd = u.size, dptr(u), 0
+        else:
+            k = 1000 if num_samples is None else int(num_samples)
+            up = None
+            sd = int(np.random.default_rng().integers(0, 2**63)) if seed is None else int(seed) % 2**64
+        nobs = len(self.observables())
+        out = np.empty(max(nobs, 1), dtype=np.float64)
+        check(lib.dmv_circuit_sample_expectation_values(self._h, up, sd, k, dptr(out)))
+        return out[:nobs]
+
     def get_fidelity_between_two_states_with_parameters(self, parameters_1, parameters_2) -> float:
         """|<psi(p1)|psi(p2)>|^2, overlap on the device; clears the gates like the reference."""
         p1 = np.ascontiguousarray(np.asarray(parameters_1, dtype=np.float64).reshape(-1))

@@ -668,6 +668,46 @@ extern "C" int dmv_sample(dmv_state_t s, const double* uniforms, int64_t k, uint
   return launch_sample(s, uniforms, k, samples);
 }
 
+namespace dmv {
+namespace {
+
+int check_uniforms(const double* uniforms, int64_t k) {
+  for (int64_t i = 0; i < k; ++i)
+    if (!(uniforms[i] >= 0.0 && uniforms[i] < 1.0))
+      return set_error(DMV_ERR_INVALID, "uniform %lld = %g outside [0,1)", (long long)i, uniforms[i]);
+  return DMV_OK;
+}
+
+int sample_expect(dmv_state_s* s, const double* uniforms, uint64_t seed, int64_t k, const int32_t* qubits,
+                  int32_t num_obs, double* means, int64_t* set_counts) {
+  if (k <= 0) return set_error(DMV_ERR_INVALID, "sampled expectation needs k >= 1 samples (got %lld)", (long long)k);
+  if (k >= (int64_t(1) << 53)) return set_error(DMV_ERR_INVALID, "k = %lld samples: at most 2^53", (long long)k);
+  if (num_obs < 0 || (num_obs > 0 && (!qubits || !means)))
+    return set_error(DMV_ERR_INVALID, "bad observable buffers");
+  for (int32_t j = 0; j < num_obs; ++j)
+    if (qubits[j] < 0 || qubits[j] >= s->n)
+      return set_error(DMV_ERR_INVALID, "observable %d: qubit %d outside [0, %d)", j, qubits[j], s->n);
+  if (uniforms) DMV_TRY(check_uniforms(uniforms, k));
+  unsigned long long counts[64];
+  DMV_TRY(launch_sample_counts(s, uniforms, seed, k, counts));
+  for (int32_t j = 0; j < num_obs; ++j) {
+    const unsigned long long c = counts[qubits[j]];
+    means[j] = (double)(k - 2 * (int64_t)c) / (double)k;
+    if (set_counts) set_counts[j] = (int64_t)c;
+  }
+  return DMV_OK;
+}
+
+}  // namespace
+}  // namespace dmv
+
+extern "C" int dmv_sample_expect_z(dmv_state_t s, const double* uniforms, uint64_t seed, int64_t k,
+                                   const int32_t* qubits, int32_t num_obs, double* means, int64_t* set_counts) {
+  clear_error();
+  DMV_TRY(check_state(s));
+  return sample_expect(s, uniforms, seed, k, qubits, num_obs, means, set_counts);
+}
+
 extern "C" int dmv_sample_probabilities(const double* probs, int64_t num_probs, const double* uniforms, int64_t k,
                                         uint64_t* samples) {
   clear_error();
@@ -920,6 +960,21 @@ extern "C" int dmv_circuit_extract_expectation_values(dmv_circuit_t c, const uin
     for (size_t j = 0; j < nobs; ++j)
       out[(size_t)s * nobs + j] = ((samples[s] >> (q[j] & 63)) & 1) ? -1. : 1.;
   return DMV_OK;
+}
+
+extern "C" int dmv_circuit_sample_expectation_values(dmv_circuit_t c, const double* uniforms, uint64_t seed,
+                                                     int64_t k, double* means) {
+  clear_error();
+  DMV_TRY(check_circuit(c));
+  const size_t nobs = c->observables.size();
+  std::vector<int32_t> q(nobs);
+  for (size_t j = 0; j < nobs; ++j) {
+    const int64_t gi = c->observables[j];
+    if (gi >= (int64_t)c->gates.size())
+      return set_error(DMV_ERR_STATE, "observable %zu refers to gate %lld, past the gate list", j, (long long)gi);
+    q[j] = c->gates[(size_t)gi].target;
+  }
+  return sample_expect(c->state, uniforms, seed, k, q.data(), (int32_t)nobs, means, nullptr);
 }
 
 extern "C" int dmv_circuit_fidelity_with_parameters(dmv_circuit_t c, const double* p1, int64_t n1, const double* p2,

@@ -47,6 +47,14 @@ __device__ __forceinline__ void apply_pair(const M2<R>& m, V& a0, V& a1) {
     b1.x = fma(m.r10, a0.x, -m.i10 * a0.y);
     b1.y = fma(m.r10, a0.y, m.i10 * a0.x);
     a0 = b0; a1 = b1;
+  } else if constexpr (CLS == OP_RXLIKE) {
+    // out0 = r00 a0 + i i01 a1, out1 = i i10 a0 + r11 a1
+    V b0, b1;
+    b0.x = fma(m.r00, a0.x, -m.i01 * a1.y);
+    b0.y = fma(m.r00, a0.y, m.i01 * a1.x);
+    b1.x = fma(m.r11, a1.x, -m.i10 * a0.y);
+    b1.y = fma(m.r11, a1.y, m.i10 * a0.x);
+    a0 = b0; a1 = b1;
   } else if constexpr (CLS == OP_REAL) {
     V b0, b1;
     b0.x = fma(m.r00, a0.x, m.r01 * a1.x);
@@ -71,6 +79,7 @@ __device__ __forceinline__ void apply_pair_dyn(int cls, const M2<R>& m, V& a0, V
     case OP_DIAG: apply_pair<R, OP_DIAG>(m, a0, a1); break;
     case OP_ANTI: apply_pair<R, OP_ANTI>(m, a0, a1); break;
     case OP_REAL: apply_pair<R, OP_REAL>(m, a0, a1); break;
+    case OP_RXLIKE: apply_pair<R, OP_RXLIKE>(m, a0, a1); break;
     default: apply_pair<R, OP_GENERAL>(m, a0, a1); break;
   }
 }

@@ -68,6 +68,7 @@ int32_t classify(const double m[8]) {
   if (off_zero) return OP_DIAG;
   if (diag_zero) return OP_ANTI;
   if (m[1] == 0. && m[3] == 0. && m[5] == 0. && m[7] == 0.) return OP_REAL;
+  if (m[1] == 0. && m[7] == 0. && m[2] == 0. && m[4] == 0.) return OP_RXLIKE;
   return OP_GENERAL;
 }
 

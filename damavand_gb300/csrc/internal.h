@@ -59,7 +59,8 @@ enum OpClass : int32_t {
   OP_DIAG = 1,     // m01 = m10 = 0
   OP_SWAP = 2,     // exactly [[0,1],[1,0]] (X, CNOT): a pure exchange
   OP_REAL = 3,     // all four entries real
-  OP_ANTI = 4      // m00 = m11 = 0 (Y and scaled exchanges)
+  OP_ANTI = 4,     // m00 = m11 = 0 (Y and scaled exchanges)
+  OP_RXLIKE = 5    // m00, m11 real and m01, m10 imaginary (RX and its adjoint): 8 multiply-adds
 };
 
 // Control kinds inside a fused pass.
@@ -292,6 +293,11 @@ int launch_plan(dmv_state_s* s, const Plan& plan);
 int launch_probabilities(dmv_state_s* s, double* probs_device);
 int launch_expect_z(dmv_state_s* s, double* expect_host, double* norm_host);
 int launch_sample(dmv_state_s* s, const double* uniforms_host, int64_t k, uint64_t* samples_host);
+// Draws k samples on the device (uniforms from the host, or from the seeded
+// SplitMix64 stream when uniforms_host is null) and counts, per bit position,
+// the samples with that bit set; the samples never leave the device.
+int launch_sample_counts(dmv_state_s* s, const double* uniforms_host, uint64_t seed, int64_t k,
+                         unsigned long long counts_host[64]);
 int sample_from_device_probs(const double* probs_device, int64_t num_probs, int32_t num_bits,
                              cudaStream_t stream, const double* uniforms_host, int64_t k,
                              uint64_t* samples_host);

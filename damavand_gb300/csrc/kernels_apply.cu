@@ -112,6 +112,7 @@ void launch_single(void* amps, int32_t n, const Op& op, cudaStream_t stream) {
     case OP_DIAG: launch_single_c<P, OP_DIAG>(a, n, op, stream); break;
     case OP_ANTI: launch_single_c<P, OP_ANTI>(a, n, op, stream); break;
     case OP_REAL: launch_single_c<P, OP_REAL>(a, n, op, stream); break;
+    case OP_RXLIKE: launch_single_c<P, OP_RXLIKE>(a, n, op, stream); break;
     default: launch_single_c<P, OP_GENERAL>(a, n, op, stream); break;
   }
 }
@@ -621,6 +622,7 @@ double op_multiply_adds(const Op& op, int64_t N, int arith) {
   const bool pair_arith = arith == ARITH_FP32X2, fixed = arith == ARITH_INT64;
   switch (op.cls) {
     case OP_GENERAL: per_pair = pair_arith ? 172. : fixed ? 64. : 16.; break;
+    case OP_RXLIKE: per_pair = pair_arith ? 172. : fixed ? 64. : 8.; break;  // general code in those arithmetics
     case OP_SWAP: per_pair = 0.; break;
     default: per_pair = pair_arith ? 76. : fixed ? 32. : 8.; break;
   }

@@ -194,65 +194,158 @@ k_scan_chunks(const double* __restrict__ mass, int64_t num_chunks, double* __res
   }
 }
 
-// One CTA per sample. Finds the least index with u*total <= cdf(index), the
-// rule of src/utils.rs:258-277 (cdf(index) = p_0 + ... + p_index).
+// Sampling works on segments of 2^seg_bits amplitudes (at most 256) inside
+// chunks of 2^chunk_bits (at most 8192: at most 32 segments per chunk). Lane
+// l of a segment's warp holds elements l*E .. l*E+E-1, E = 2^(seg_bits-5)
+// (one element, and idle lanes, below 32 amplitudes).
+__device__ __forceinline__ int seg_lane_elems(int seg_bits) { return seg_bits >= 5 ? 1 << (seg_bits - 5) : 1; }
+
+// Per chunk c: seg_incl[c * spc + j] = t_0 + ... + t_j (in segment order),
+// t_j the probability mass of segment j, and chunk_mass[c] = the chunk's last
+// seg_incl. One warp per chunk; lane l sums elements l, l + 32, ... of a
+// segment (coalesced loads), then a shuffle tree gives t_j to every lane.
 template <int SRC>
 __global__ void __launch_bounds__(kRedThreads)
-k_sample(const void* src, int chunk_bits, int64_t num_chunks, const double* __restrict__ incl,
-         const double* __restrict__ uniforms, int64_t k, uint64_t* __restrict__ samples) {
-  __shared__ double scan[kRedThreads];
-  __shared__ long long best;
-  __shared__ long long last_nonzero;
-  const int C = 1 << chunk_bits;
-  const double total = incl[num_chunks - 1];
-  for (int64_t s = blockIdx.x; s < k; s += gridDim.x) {
+k_segment_prefix(const void* src, int seg_bits, int chunk_bits, int64_t num_chunks, double* __restrict__ seg_incl,
+                 double* __restrict__ chunk_mass) {
+  const int lane = threadIdx.x & 31;
+  const int S = 1 << seg_bits, spc = 1 << (chunk_bits - seg_bits);
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += nwarps) {
+    double run = 0.;
+    for (int j = 0; j < spc; ++j) {
+      const int64_t base = (c << chunk_bits) + ((int64_t)j << seg_bits);
+      double ls = 0.;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        if (lane + 32 * e < S) ls += prob_at<SRC>(src, base + lane + 32 * e);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, off);
+      run += ls;
+      if (lane == 0) seg_incl[c * spc + j] = run;
+    }
+    if (lane == 0) chunk_mass[c] = run;
+  }
+}
+
+// One warp per sample: the least index with u*total <= cdf(index), the rule
+// of src/utils.rs:258-277 (cdf(index) = p_0 + ... + p_index), through the
+// prefix levels: the chunk by binary search on the chunk prefixes, the segment
+// by a ballot over the chunk's segment prefixes, the element by a scan of the
+// segment (lane sums, a shuffle scan, then each lane's own elements in order).
+// Where rounding between the levels leaves no element of the chosen segment
+// reaching u*total, the segment's last element of nonzero probability is taken
+// (the chosen segment has nonzero mass, so one exists).
+template <int SRC>
+__global__ void __launch_bounds__(kRedThreads)
+k_sample_warp(const void* src, int seg_bits, int chunk_bits, int64_t num_chunks, const double* __restrict__ chunk_incl,
+              const double* __restrict__ seg_incl, const double* __restrict__ uniforms, int64_t k,
+              uint64_t* __restrict__ samples) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int S = 1 << seg_bits, E = seg_lane_elems(seg_bits), spc = 1 << (chunk_bits - seg_bits);
+  const double total = chunk_incl[num_chunks - 1];
+  for (int64_t s = warp0; s < k; s += nwarps) {
     const double xsi = uniforms[s] * total;
     if (!(xsi > 0.)) {  // xsi == 0 matches cdf[0] = 0: the reference returns 0 - 1
-      if (threadIdx.x == 0) samples[s] = ~uint64_t(0);
+      if (lane == 0) samples[s] = ~uint64_t(0);
       continue;
     }
-    // least chunk whose inclusive mass reaches xsi
-    int64_t lo = 0, hi = num_chunks - 1;
+    int64_t lo = 0, hi = num_chunks - 1;  // least chunk whose inclusive mass reaches xsi
     while (lo < hi) {
       const int64_t mid = lo + (hi - lo) / 2;
-      if (xsi <= incl[mid]) hi = mid; else lo = mid + 1;
+      if (xsi <= chunk_incl[mid]) hi = mid;
+      else lo = mid + 1;
     }
-    const int64_t ch = lo;
-    const double before = ch > 0 ? incl[ch - 1] : 0.;
-    const int per = (C + kRedThreads - 1) / kRedThreads;
-    const int64_t base = (ch << chunk_bits);
-    const int e0 = threadIdx.x * per;
-    double mine = 0.;
-    for (int j = 0; j < per; ++j)
-      if (e0 + j < C) mine += prob_at<SRC>(src, base + e0 + j);
-    scan[threadIdx.x] = mine;
-    if (threadIdx.x == 0) { best = LLONG_MAX; last_nonzero = -1; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double run = 0.;
-      for (int t = 0; t < kRedThreads; ++t) { const double x = scan[t]; scan[t] = run; run += x; }
+    const double before = lo > 0 ? chunk_incl[lo - 1] : 0.;
+    const double* sp = seg_incl + lo * spc;
+    const unsigned segs = __ballot_sync(0xffffffffu, lane < spc && xsi <= before + sp[lane < spc ? lane : 0]);
+    const int sg = segs ? __ffs((int)segs) - 1 : spc - 1;
+    const double sbefore = sg > 0 ? before + sp[sg - 1] : before;
+    const int64_t base = ((lo * spc + sg) << seg_bits) + (int64_t)lane * E;
+    const int mine = lane * E < S ? E : 0;
+    double p[8];
+    double ls = 0.;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      p[e] = e < mine ? prob_at<SRC>(src, base + e) : 0.;
+      ls += p[e];
     }
-    __syncthreads();
-    double run = before + scan[threadIdx.x];
-    long long found = LLONG_MAX, nz = -1;
-    for (int j = 0; j < per; ++j) {
-      const int e = e0 + j;
-      if (e >= C) break;
-      const double p = prob_at<SRC>(src, base + e);
-      run += p;
-      if (p > 0.) nz = base + e;
-      if (xsi <= run) { found = base + e; break; }
+    double incl = ls;  // inclusive scan of the lane sums
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += t;
     }
-    if (found != LLONG_MAX) atomicMin(&best, found);
-    if (nz >= 0) atomicMax(&last_nonzero, nz);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      long long r = best;
-      if (r == LLONG_MAX) r = last_nonzero >= 0 ? last_nonzero : (long long)(base + C - 1);
-      samples[s] = (uint64_t)r;
+    const double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    double run = sbefore + (lane > 0 ? excl : 0.);
+    int hit = -1, last_nz = -1;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      if (e < mine) {
+        run += p[e];
+        if (p[e] > 0.) last_nz = e;
+        if (hit < 0 && xsi <= run) hit = e;
+      }
     }
-    __syncthreads();
+    const unsigned hits = __ballot_sync(0xffffffffu, hit >= 0);
+    const int64_t seg_base = (lo * spc + sg) << seg_bits;
+    if (hits) {
+      const int l = __ffs((int)hits) - 1;
+      const int e = __shfl_sync(0xffffffffu, hit, l);
+      if (lane == 0) samples[s] = (uint64_t)(seg_base + (int64_t)l * E + e);
+    } else {
+      const unsigned nz = __ballot_sync(0xffffffffu, last_nz >= 0);
+      const int l = nz ? 31 - __clz((int)nz) : -1;
+      const int e = __shfl_sync(0xffffffffu, last_nz, l >= 0 ? l : 0);
+      if (lane == 0) samples[s] = (uint64_t)(l >= 0 ? seg_base + (int64_t)l * E + e : seg_base + S - 1);
+    }
   }
+}
+
+// Uniform i of the seeded device stream: SplitMix64 (Steele, Lea and Flood,
+// "Fast splittable pseudorandom number generators", OOPSLA 2014) of the
+// counter state seed + (i + 1) * 0x9E3779B97F4A7C15, its top 53 bits scaled
+// by 2^-53, so every value lies in [0, 1).
+__device__ __forceinline__ double splitmix_uniform(uint64_t seed, uint64_t i) {
+  uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * 0x1.0p-53;
+}
+
+__global__ void k_uniforms(uint64_t seed, int64_t first, int64_t count, double* __restrict__ u) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+    u[i] = splitmix_uniform(seed, (uint64_t)(first + i));
+}
+
+// counts[b] += number of samples with bit b set, b = 0 .. 63 (a sample of
+// ~0, the reference's 0 - 1, has every bit set). Each warp takes 32 samples
+// at a time and one ballot per bit; lane b keeps the counts of bits b and
+// b + 32. Integer atomics: the totals do not depend on the order.
+__global__ void __launch_bounds__(kRedThreads)
+k_count_bits(const uint64_t* __restrict__ samples, int64_t k, unsigned long long* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long lo = 0, hi = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < k; i0 += stride) {
+    const int64_t i = i0 + lane;
+    const uint64_t x = i < k ? samples[i] : 0ull;  // lanes past the end set no bit
+#pragma unroll
+    for (int b = 0; b < 32; ++b) {
+      const unsigned bl = __ballot_sync(0xffffffffu, (unsigned)(x >> b) & 1u);
+      const unsigned bh = __ballot_sync(0xffffffffu, (unsigned)(x >> (b + 32)) & 1u);
+      if (lane == b) {
+        lo += (unsigned)__popc(bl);
+        hi += (unsigned)__popc(bh);
+      }
+    }
+  }
+  if (lo) atomicAdd(&counts[lane], lo);
+  if (hi) atomicAdd(&counts[lane + 32], hi);
 }
 
 template <typename V>
@@ -384,25 +477,64 @@ int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& chunk_de
   return DMV_OK;
 }
 
-int run_sampler(const void* src, int src_kind, int chunk_bits, int64_t num_chunks,
-                const double* mass, DeviceBuffer& scratch, cudaStream_t stream,
-                const double* uniforms_host, int64_t k, uint64_t* samples_host) {
-  if (k <= 0) return DMV_OK;
-  const size_t need = (size_t)num_chunks * sizeof(double) + (size_t)k * (sizeof(double) + sizeof(uint64_t));
-  DMV_TRY(scratch.reserve(need));
-  double* incl = static_cast<double*>(scratch.ptr);
-  double* u_dev = incl + num_chunks;
-  uint64_t* out_dev = reinterpret_cast<uint64_t*>(u_dev + k);
-  DMV_CUDA_TRY(cudaMemcpyAsync(u_dev, uniforms_host, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, stream));
-  k_scan_chunks<<<1, 1024, 0, stream>>>(mass, num_chunks, incl);
-  const int grid = (int)std::min<int64_t>(k, (int64_t)sm_count() * 8);
+// Prefix levels of the sampler, in `prefix`: chunk masses, their inclusive
+// scan, then the per-chunk segment prefixes.
+struct SamplePrefix {
+  int seg_bits = 0, chunk_bits = 0;
+  int64_t num_chunks = 0;
+  const double* chunk_incl = nullptr;
+  const double* seg_incl = nullptr;
+};
+
+int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefix, cudaStream_t stream,
+                       SamplePrefix* out) {
+  SamplePrefix sp;
+  sp.seg_bits = std::min(8, n);
+  sp.chunk_bits = chunk_bits_for(n);
+  sp.num_chunks = int64_t(1) << (n - sp.chunk_bits);
+  const int64_t nseg = int64_t(1) << (n - sp.seg_bits);
+  DMV_TRY(prefix.reserve((size_t)(2 * sp.num_chunks + nseg) * sizeof(double)));
+  double* mass = static_cast<double*>(prefix.ptr);
+  double* incl = mass + sp.num_chunks;
+  double* seg = incl + sp.num_chunks;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 7) / 8, (int64_t)sm_count() * 8));
   switch (src_kind) {
-    case 0: k_sample<0><<<grid, kRedThreads, 0, stream>>>(src, chunk_bits, num_chunks, incl, u_dev, k, out_dev); break;
-    case 1: k_sample<1><<<grid, kRedThreads, 0, stream>>>(src, chunk_bits, num_chunks, incl, u_dev, k, out_dev); break;
-    default: k_sample<2><<<grid, kRedThreads, 0, stream>>>(src, chunk_bits, num_chunks, incl, u_dev, k, out_dev); break;
+    case 0: k_segment_prefix<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+    case 1: k_segment_prefix<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+    default: k_segment_prefix<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
   }
+  k_scan_chunks<<<1, 1024, 0, stream>>>(mass, sp.num_chunks, incl);
   count_launch(2);
   DMV_CUDA_TRY(cudaGetLastError());
+  sp.chunk_incl = incl;
+  sp.seg_incl = seg;
+  *out = sp;
+  return DMV_OK;
+}
+
+int launch_warp_sampler(const void* src, int src_kind, const SamplePrefix& sp, const double* u_dev, int64_t k,
+                        uint64_t* out_dev, cudaStream_t stream) {
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((k + 7) / 8, (int64_t)sm_count() * 8));
+  switch (src_kind) {
+    case 0: k_sample_warp<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.seg_incl, u_dev, k, out_dev); break;
+    case 1: k_sample_warp<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.seg_incl, u_dev, k, out_dev); break;
+    default: k_sample_warp<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.seg_incl, u_dev, k, out_dev); break;
+  }
+  count_launch();
+  DMV_CUDA_TRY(cudaGetLastError());
+  return DMV_OK;
+}
+
+int run_sampler(const void* src, int src_kind, int n, DeviceBuffer& prefix, DeviceBuffer& scratch,
+                cudaStream_t stream, const double* uniforms_host, int64_t k, uint64_t* samples_host) {
+  if (k <= 0) return DMV_OK;
+  SamplePrefix sp;
+  DMV_TRY(sample_prefix_pass(src, src_kind, n, prefix, stream, &sp));
+  DMV_TRY(scratch.reserve((size_t)k * (sizeof(double) + sizeof(uint64_t))));
+  double* u_dev = static_cast<double*>(scratch.ptr);
+  uint64_t* out_dev = reinterpret_cast<uint64_t*>(u_dev + k);
+  DMV_CUDA_TRY(cudaMemcpyAsync(u_dev, uniforms_host, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, stream));
+  DMV_TRY(launch_warp_sampler(src, src_kind, sp, u_dev, k, out_dev, stream));
   DMV_CUDA_TRY(cudaMemcpyAsync(samples_host, out_dev, (size_t)k * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
   DMV_CUDA_TRY(cudaStreamSynchronize(stream));
   return DMV_OK;
@@ -462,30 +594,58 @@ int launch_expect_z(dmv_state_s* s, double* expect_host, double* norm_host) {
 }
 
 int launch_sample(dmv_state_s* s, const double* uniforms_host, int64_t k, uint64_t* samples_host) {
-  double* sums = nullptr;
-  int64_t nc = 0;
-  int cb = 0;
+  return run_sampler(s->amps, s->precision == DMV_C128 ? 0 : 1, s->n, s->chunk_dev, s->reduce_dev, s->stream,
+                     uniforms_host, k, samples_host);
+}
+
+// Samples per batch of the sampled-expectation pipeline (uniforms and samples
+// of a batch: 256 MB of scratch).
+constexpr int64_t kSampleBatch = int64_t(1) << 24;
+
+int launch_sample_counts(dmv_state_s* s, const double* uniforms_host, uint64_t seed, int64_t k,
+                         unsigned long long counts_host[64]) {
+  for (int b = 0; b < 64; ++b) counts_host[b] = 0;
+  if (k <= 0) return DMV_OK;
   const int src_kind = s->precision == DMV_C128 ? 0 : 1;
-  DMV_TRY(chunk_mass_pass(s->amps, src_kind, s->n, s->chunk_dev, s->reduce_dev, s->stream, &sums, &nc, &cb));
-  return run_sampler(s->amps, src_kind, cb, nc, static_cast<const double*>(s->chunk_dev.ptr), s->reduce_dev,
-                     s->stream, uniforms_host, k, samples_host);
+  SamplePrefix sp;
+  DMV_TRY(sample_prefix_pass(s->amps, src_kind, s->n, s->chunk_dev, s->stream, &sp));
+  const int64_t batch = std::min<int64_t>(k, kSampleBatch);
+  DMV_TRY(s->reduce_dev.reserve((size_t)batch * (sizeof(double) + sizeof(uint64_t)) + 64 * sizeof(unsigned long long)));
+  double* u_dev = static_cast<double*>(s->reduce_dev.ptr);
+  uint64_t* out_dev = reinterpret_cast<uint64_t*>(u_dev + batch);
+  unsigned long long* counts_dev = reinterpret_cast<unsigned long long*>(out_dev + batch);
+  DMV_CUDA_TRY(cudaMemsetAsync(counts_dev, 0, 64 * sizeof(unsigned long long), s->stream));
+  for (int64_t off = 0; off < k; off += batch) {
+    const int64_t cnt = std::min(batch, k - off);
+    if (uniforms_host) {
+      DMV_CUDA_TRY(cudaMemcpyAsync(u_dev, uniforms_host + off, (size_t)cnt * sizeof(double), cudaMemcpyHostToDevice,
+                                   s->stream));
+    } else {
+      const int ug = (int)std::max<int64_t>(1, std::min<int64_t>((cnt + 255) / 256, (int64_t)sm_count() * 8));
+      k_uniforms<<<ug, 256, 0, s->stream>>>(seed, off, cnt, u_dev);
+      count_launch();
+    }
+    DMV_TRY(launch_warp_sampler(s->amps, src_kind, sp, u_dev, cnt, out_dev, s->stream));
+    const int cg = (int)std::max<int64_t>(1, std::min<int64_t>((cnt + kRedThreads - 1) / kRedThreads,
+                                                               (int64_t)sm_count() * 8));
+    k_count_bits<<<cg, kRedThreads, 0, s->stream>>>(out_dev, cnt, counts_dev);
+    count_launch();
+    DMV_CUDA_TRY(cudaGetLastError());
+  }
+  DMV_CUDA_TRY(cudaMemcpyAsync(counts_host, counts_dev, 64 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               s->stream));
+  DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return DMV_OK;
 }
 
 int sample_from_device_probs(const double* probs_device, int64_t num_probs, int32_t num_bits,
                              cudaStream_t stream, const double* uniforms_host, int64_t k,
                              uint64_t* samples_host) {
   (void)num_probs;
-  DeviceBuffer chunk_dev, reduce_dev, scratch;
-  double* sums = nullptr;
-  int64_t nc = 0;
-  int cb = 0;
-  int rc = chunk_mass_pass(probs_device, 2, num_bits, chunk_dev, reduce_dev, stream, &sums, &nc, &cb);
-  if (rc == DMV_OK)
-    rc = run_sampler(probs_device, 2, cb, nc, static_cast<const double*>(chunk_dev.ptr), scratch, stream,
-                     uniforms_host, k, samples_host);
+  DeviceBuffer prefix, scratch;
+  const int rc = run_sampler(probs_device, 2, num_bits, prefix, scratch, stream, uniforms_host, k, samples_host);
   cudaStreamSynchronize(stream);
-  chunk_dev.release();
-  reduce_dev.release();
+  prefix.release();
   scratch.release();
   return rc;
 }

@@ -122,6 +122,7 @@ __device__ __forceinline__ void regs_apply_op(typename P::T (&r)[1 << RB], const
     case OP_DIAG: regs_apply_tp<P, OP_DIAG, RB>(r, m, tp, cmask); break;
     case OP_ANTI: regs_apply_tp<P, OP_ANTI, RB>(r, m, tp, cmask); break;
     case OP_REAL: regs_apply_tp<P, OP_REAL, RB>(r, m, tp, cmask); break;
+    case OP_RXLIKE: regs_apply_tp<P, OP_RXLIKE, RB>(r, m, tp, cmask); break;
     default: regs_apply_tp<P, OP_GENERAL, RB>(r, m, tp, cmask); break;
   }
 }

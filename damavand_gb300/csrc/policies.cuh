@@ -120,6 +120,7 @@ __device__ __forceinline__ void apply_dyn(int cls, const typename P::Mat& m, typ
     case OP_DIAG: P::template apply<OP_DIAG>(m, a0, a1); break;
     case OP_ANTI: P::template apply<OP_ANTI>(m, a0, a1); break;
     case OP_REAL: P::template apply<OP_REAL>(m, a0, a1); break;
+    case OP_RXLIKE: P::template apply<OP_RXLIKE>(m, a0, a1); break;
     default: P::template apply<OP_GENERAL>(m, a0, a1); break;
   }
 }
@@ -314,6 +315,7 @@ __device__ __forceinline__ void tile_apply_ops(typename P::T* tile, int T, const
       case OP_DIAG: tile_op<P, OP_DIAG>(tile, T, op); break;
       case OP_ANTI: tile_op<P, OP_ANTI>(tile, T, op); break;
       case OP_REAL: tile_op<P, OP_REAL>(tile, T, op); break;
+      case OP_RXLIKE: tile_op<P, OP_RXLIKE>(tile, T, op); break;
       default: tile_op<P, OP_GENERAL>(tile, T, op); break;
     }
     __syncthreads();

@@ -201,6 +201,18 @@ int dmv_sample(dmv_state_t s, const double* uniforms, int64_t k, uint64_t* sampl
 /* Same rule on a caller-supplied host probability vector (Circuit.sample_local). */
 int dmv_sample_probabilities(const double* probs, int64_t num_probs, const double* uniforms,
                              int64_t k, uint64_t* samples);
+/* Sampled expectation values, samples kept on the device: k samples drawn by
+ * dmv_sample's rule, then for each of the num_obs qubits the mean over the
+ * samples of +1 (bit clear) / -1 (bit set): the per-sample values of
+ * extract_expectation_values (src/qubit_backend/circuit.rs:494-513) averaged,
+ * without moving the samples to the host. `uniforms`: k host values in
+ * [0,1), or NULL to draw them on the device from `seed` (SplitMix64: uniform
+ * i = (mix64(seed + (i+1) * 0x9E3779B97F4A7C15) >> 11) * 2^-53). `set_counts`
+ * (may be NULL) receives, per qubit, the number of samples with the bit set;
+ * means[j] = (k - 2 set_counts[j]) / k exactly. k is processed in batches of
+ * 2^24 (256 MB of scratch). */
+int dmv_sample_expect_z(dmv_state_t s, const double* uniforms, uint64_t seed, int64_t k,
+                        const int32_t* qubits, int32_t num_obs, double* means, int64_t* set_counts);
 /* <a|b> (conjugate-linear in a), FP64 accumulation. */
 int dmv_inner_product(dmv_state_t a, dmv_state_t b, double* re, double* im);
 
@@ -298,6 +310,11 @@ int dmv_circuit_observables(dmv_circuit_t c, int32_t* readout_qubits);
 /* out[s*num_obs + j] = -1 if bit readout_j of samples[s] is set else +1 (circuit.rs:494-513). */
 int dmv_circuit_extract_expectation_values(dmv_circuit_t c, const uint64_t* samples, int64_t k,
                                            double* out);
+/* dmv_sample_expect_z over the circuit's observables (their readout qubits,
+ * in the order they were added): means[j] is the average over k device-drawn
+ * samples of column j of extract_expectation_values. */
+int dmv_circuit_sample_expectation_values(dmv_circuit_t c, const double* uniforms, uint64_t seed, int64_t k,
+                                          double* means);
 /* |<psi(params1)|psi(params2)>|^2; clears the gate list afterwards like
  * the reference's get_fidelity (circuit_metrics.rs:11-32). */
 int dmv_circuit_fidelity_with_parameters(dmv_circuit_t c, const double* p1, int64_t n1,

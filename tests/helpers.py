@@ -42,6 +42,25 @@ def assert_samples_match(probs, uniforms, got, oracle_mod):
     return int(mism.size)
 
 
+SPLITMIX_GAMMA = 0x9E3779B97F4A7C15
+
+
+def splitmix64(seed, first, k):
+    """Outputs first .. first+k-1 of SplitMix64 (Steele, Lea and Flood, OOPSLA
+    2014) started at `seed`: mix(seed + (i + 1) * gamma), numpy uint64 (wraps mod 2^64)."""
+    with np.errstate(over="ignore"):
+        i = np.arange(first, first + k, dtype=np.uint64)
+        z = np.uint64(seed % 2**64) + (i + np.uint64(1)) * np.uint64(SPLITMIX_GAMMA)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def splitmix_uniforms(seed, k, first=0):
+    """The device stream of dmv_sample_expect_z: top 53 bits of SplitMix64 times 2^-53."""
+    return (splitmix64(seed, first, k) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+
 def random_state(n, rng):
     v = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
     return v / np.linalg.norm(v)
