@@ -4,11 +4,12 @@
 
 On an n-qubit complex128 state (and a complex64 copy) it launches, in order:
 the single-op pass (general, controlled), the window pass (FP64, FP32-pair,
-int64, tensor-core digit products, complex64), the probability kernel, the Pauli-Z / chunk-mass reduction, the
-sampler, the inner product, the observable scaling and the adjoint step (one
-small adjoint), the layout conversions of a host copy, the allocation-free
-expectation, and one batched persistent launch. Each prints its wall time so
-a plain run shows the tour completed.
+int64, tensor-core digit products, complex64), the probability kernel, the
+Pauli-Z / chunk-mass reduction, the sampler (1000 host-uniform samples, then
+2^20 seeded samples counted on the device), the inner product, the observable
+scaling and the adjoint step (one small adjoint), the layout conversions of a
+host copy, the allocation-free expectation, and one batched persistent
+launch. Each prints its wall time so a plain run shows the tour completed.
 """
 from __future__ import annotations
 
@@ -27,7 +28,7 @@ from .workloads import gate_array, ladder_circuit, loss_weights, ring_ansatz, un
 def _timed(label, fn):
     t0 = time.perf_counter()
     fn()
-    print(f"{label:28s} {1e3 * (time.perf_counter() - t0):9.2f} ms", flush=True)
+    print(f"{label:50s} {1e3 * (time.perf_counter() - t0):9.2f} ms", flush=True)
 
 
 def main():
@@ -63,6 +64,10 @@ def main():
     _timed("expectation (chunk mass)", lambda: c.expectation_z())
     u = np.random.default_rng(0).random(1000)
     _timed("sample 1000", lambda: c.sample_array(1000, uniforms=u))
+    qs = np.arange(n, dtype=np.int32)
+    means = np.empty(n)
+    _timed("sampled expectation (2^20 samples on the device)", lambda: check(lib.dmv_sample_expect_z(
+        st.handle, None, 7, 1 << 20, qs.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), n, dptr(means), None)))
     other = Circuit(n)
     re, im = ctypes.c_double(), ctypes.c_double()
     _timed("inner product", lambda: check(lib.dmv_inner_product(st.handle, other.state().handle,
