@@ -231,9 +231,23 @@ def cpu_baseline(args):
         oracle.forward(n, [gates[done]], state)
         done += 1
     el = time.perf_counter() - t0
+    cores = oracle.num_threads()
+    # the same port on one host core: the next gate of the forward
+    single = None
+    if done < len(gates):
+        oracle.set_num_threads(1)
+        try:
+            t1 = time.perf_counter()
+            oracle.forward(n, [gates[done]], state)
+            el1 = time.perf_counter() - t1
+        finally:
+            oracle.set_num_threads(cores)
+        single = {"value": 1.0 / el1, "unit": UNIT, "cores": 1,
+                  "sample": f"gate {done + 1} of the same forward on one thread ({el1:.1f} s)"}
     del state
-    return {"value": done / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"first {done} gates of the {len(gates)}-gate {n}-qubit forward ({el:.1f} s)"}
+    return {"value": done / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {done} gates of the {len(gates)}-gate {n}-qubit forward ({el:.1f} s)",
+            "single_core": single}
 
 
 def adjoint_section(args):
