@@ -204,6 +204,21 @@ __device__ __forceinline__ int seg_lane_elems(int seg_bits) { return seg_bits >=
 // t_j the probability mass of segment j, and chunk_mass[c] = the chunk's last
 // seg_incl. One warp per chunk; lane l sums elements l, l + 32, ... of a
 // segment (coalesced loads), then a shuffle tree gives t_j to every lane.
+// acc + |a_i|^2 as two chained FP64 multiply-adds (the square is not rounded
+// on its own): the FP64 pipe, not HBM, bounds a pass over the state.
+template <int SRC>
+__device__ __forceinline__ double prob_acc(const void* src, int64_t i, double acc) {
+  if constexpr (SRC == 0) {
+    const double2 v = static_cast<const double2*>(src)[i];
+    return fma(v.y, v.y, fma(v.x, v.x, acc));
+  } else if constexpr (SRC == 1) {
+    const float2 v = static_cast<const float2*>(src)[i];
+    return fma((double)v.y, (double)v.y, fma((double)v.x, (double)v.x, acc));
+  } else {
+    return acc + static_cast<const double*>(src)[i];
+  }
+}
+
 template <int SRC>
 __global__ void __launch_bounds__(kRedThreads)
 k_segment_prefix(const void* src, int seg_bits, int chunk_bits, int64_t num_chunks, double* __restrict__ seg_incl,
@@ -218,13 +233,37 @@ k_segment_prefix(const void* src, int seg_bits, int chunk_bits, int64_t num_chun
       double ls = 0.;
 #pragma unroll
       for (int e = 0; e < 8; ++e)
-        if (lane + 32 * e < S) ls += prob_at<SRC>(src, base + lane + 32 * e);
+        if (lane + 32 * e < S) ls = prob_acc<SRC>(src, base + lane + 32 * e, ls);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, off);
       run += ls;
       if (lane == 0) seg_incl[c * spc + j] = run;
     }
     if (lane == 0) chunk_mass[c] = run;
+  }
+}
+
+// Guide table of the chunk prefixes: guide[b] = least chunk c with
+// incl[c] >= b * (total / M) for b < M, guide[M] = the last chunk. A value
+// xsi with b * step <= xsi < (b + 1) * step has its chunk in
+// [guide[b], guide[b + 1]] (the prefixes do not decrease).
+__global__ void k_chunk_guide(const double* __restrict__ incl, int64_t num_chunks, int64_t M,
+                              int32_t* __restrict__ guide) {
+  const double step = incl[num_chunks - 1] / (double)M;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b <= M; b += stride) {
+    if (b == M) {
+      guide[b] = (int32_t)(num_chunks - 1);
+      continue;
+    }
+    const double t = (double)b * step;
+    int64_t lo = 0, hi = num_chunks - 1;
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo) / 2;
+      if (t <= incl[mid]) hi = mid;
+      else lo = mid + 1;
+    }
+    guide[b] = (int32_t)lo;
   }
 }
 
@@ -239,20 +278,29 @@ k_segment_prefix(const void* src, int seg_bits, int chunk_bits, int64_t num_chun
 template <int SRC>
 __global__ void __launch_bounds__(kRedThreads)
 k_sample_warp(const void* src, int seg_bits, int chunk_bits, int64_t num_chunks, const double* __restrict__ chunk_incl,
-              const double* __restrict__ seg_incl, const double* __restrict__ uniforms, int64_t k,
-              uint64_t* __restrict__ samples) {
+              const int32_t* __restrict__ guide, const double* __restrict__ seg_incl,
+              const double* __restrict__ uniforms, int64_t k, uint64_t* __restrict__ samples) {
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int S = 1 << seg_bits, E = seg_lane_elems(seg_bits), spc = 1 << (chunk_bits - seg_bits);
   const double total = chunk_incl[num_chunks - 1];
+  const int64_t M = num_chunks;  // guide buckets
+  const double step = total / (double)M;
   for (int64_t s = warp0; s < k; s += nwarps) {
     const double xsi = uniforms[s] * total;
     if (!(xsi > 0.)) {  // xsi == 0 matches cdf[0] = 0: the reference returns 0 - 1
       if (lane == 0) samples[s] = ~uint64_t(0);
       continue;
     }
-    int64_t lo = 0, hi = num_chunks - 1;  // least chunk whose inclusive mass reaches xsi
+    // bucket b with b * step <= xsi < (b + 1) * step (the products as the guide
+    // table computed them), then the least chunk whose inclusive mass
+    // reaches xsi, between guide[b] and guide[b + 1]
+    int64_t b = (int64_t)(xsi / step);
+    b = b < 0 ? 0 : (b >= M ? M - 1 : b);
+    while (b > 0 && (double)b * step > xsi) --b;
+    while (b + 1 < M && (double)(b + 1) * step <= xsi) ++b;
+    int64_t lo = guide[b], hi = guide[b + 1];
     while (lo < hi) {
       const int64_t mid = lo + (hi - lo) / 2;
       if (xsi <= chunk_incl[mid]) hi = mid;
@@ -483,6 +531,7 @@ struct SamplePrefix {
   int seg_bits = 0, chunk_bits = 0;
   int64_t num_chunks = 0;
   const double* chunk_incl = nullptr;
+  const int32_t* guide = nullptr;  // num_chunks + 1 entries
   const double* seg_incl = nullptr;
 };
 
@@ -493,10 +542,12 @@ int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefi
   sp.chunk_bits = chunk_bits_for(n);
   sp.num_chunks = int64_t(1) << (n - sp.chunk_bits);
   const int64_t nseg = int64_t(1) << (n - sp.seg_bits);
-  DMV_TRY(prefix.reserve((size_t)(2 * sp.num_chunks + nseg) * sizeof(double)));
+  DMV_TRY(prefix.reserve((size_t)(2 * sp.num_chunks + nseg) * sizeof(double) +
+                         (size_t)(sp.num_chunks + 1) * sizeof(int32_t)));
   double* mass = static_cast<double*>(prefix.ptr);
   double* incl = mass + sp.num_chunks;
   double* seg = incl + sp.num_chunks;
+  int32_t* guide = reinterpret_cast<int32_t*>(seg + nseg);
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 7) / 8, (int64_t)sm_count() * 8));
   switch (src_kind) {
     case 0: k_segment_prefix<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
@@ -504,9 +555,12 @@ int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefi
     default: k_segment_prefix<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
   }
   k_scan_chunks<<<1, 1024, 0, stream>>>(mass, sp.num_chunks, incl);
-  count_launch(2);
+  const int gg = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 256) / 256, (int64_t)sm_count() * 4));
+  k_chunk_guide<<<gg, 256, 0, stream>>>(incl, sp.num_chunks, sp.num_chunks, guide);
+  count_launch(3);
   DMV_CUDA_TRY(cudaGetLastError());
   sp.chunk_incl = incl;
+  sp.guide = guide;
   sp.seg_incl = seg;
   *out = sp;
   return DMV_OK;
@@ -516,9 +570,9 @@ int launch_warp_sampler(const void* src, int src_kind, const SamplePrefix& sp, c
                         uint64_t* out_dev, cudaStream_t stream) {
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((k + 7) / 8, (int64_t)sm_count() * 8));
   switch (src_kind) {
-    case 0: k_sample_warp<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.seg_incl, u_dev, k, out_dev); break;
-    case 1: k_sample_warp<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.seg_incl, u_dev, k, out_dev); break;
-    default: k_sample_warp<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.seg_incl, u_dev, k, out_dev); break;
+    case 0: k_sample_warp<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.guide, sp.seg_incl, u_dev, k, out_dev); break;
+    case 1: k_sample_warp<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.guide, sp.seg_incl, u_dev, k, out_dev); break;
+    default: k_sample_warp<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, sp.chunk_incl, sp.guide, sp.seg_incl, u_dev, k, out_dev); break;
   }
   count_launch();
   DMV_CUDA_TRY(cudaGetLastError());
