@@ -1,8 +1,9 @@
 // Reductions over the statevector: probabilities, Pauli-Z expectations with
-// per-chunk probability mass, inverse-CDF sampling, inner products, the
-// Z-observable scaling and the adjoint sweep step. All sums accumulate in
-// FP64 (also for complex64 storage) in a fixed order, so results are
-// reproducible run to run.
+// per-chunk probability mass, inverse-CDF sampling (segment and chunk
+// prefixes, a chunk guide table, one warp per sample), sampled expectation
+// values counted on the device, inner products, the Z-observable scaling and
+// the adjoint sweep step. All sums accumulate in FP64 (also for complex64
+// storage) in a fixed order, so results are reproducible run to run.
 #include <algorithm>
 #include <climits>
 #include <cmath>
