@@ -100,3 +100,66 @@ def test_reference_import_name(built_lib):
                  "get_fidelity_between_two_states_with_parameters"):
         assert callable(getattr(Circuit, name)), name
     damavand.initialize_mpi()
+
+
+_HANDLE_TYPES = ("dmv_state_t", "dmv_circuit_t", "dmv_batch_t")
+
+
+def _c_category(decl):
+    """pointer / f64 / i64 / i32 for one C parameter or return type."""
+    d = re.sub(r"\b(const|struct|unsigned|signed)\b", " ", decl).strip()
+    if "*" in d or "[" in d or any(h in d for h in _HANDLE_TYPES):  # arrays decay to pointers
+        return "ptr"
+    if "double" in d:
+        return "f64"
+    if re.search(r"\b(u?int64_t|size_t|long\s+long)\b", d):
+        return "i64"
+    if re.search(r"\b(u?int32_t|int|bool)\b", d):
+        return "i32"
+    raise AssertionError(f"unmapped C type: {decl!r}")
+
+
+def _ctypes_category(t):
+    if t is None:
+        return "void"
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "_type_") and isinstance(t._type_, type):
+        return "ptr"
+    if t is ctypes.c_double:
+        return "f64"
+    if ctypes.sizeof(t) == 8:
+        return "i64"
+    if ctypes.sizeof(t) in (4, 1):
+        return "i32"
+    raise AssertionError(f"unmapped ctypes type: {t!r}")
+
+
+def declared_signatures():
+    """name -> (return category, [parameter categories]) from the header."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for m in re.finditer(r"^\s*((?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**)\s*([a-z_][a-z0-9_]*)\s*\(([^)]*)\)\s*;",
+                         text, flags=re.M):
+        ret, name, params = m.group(1), m.group(2), " ".join(m.group(3).split())
+        plist = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+        rcat = "void" if ret.strip() == "void" else _c_category(ret)
+        out[name] = (rcat, [_c_category(p) for p in plist])
+    return out
+
+
+def test_python_bindings_match_header_signatures(built_lib):
+    """Each ctypes entry has the header's parameter count and, per parameter,
+    the same kind (pointer, 32-bit integer, 64-bit integer, double)."""
+    from damavand_gb300 import _lib
+    decl = declared_signatures()
+    assert set(decl) == set(_lib.SIGNATURES)
+    bad = []
+    for name, (restype, argtypes) in _lib.SIGNATURES.items():
+        rcat, pcats = decl[name]
+        got = [_ctypes_category(t) for t in argtypes]
+        if got != pcats:
+            bad.append((name, pcats, got))
+        if rcat != "void" and _ctypes_category(restype) != rcat:
+            bad.append((name, "returns", rcat, _ctypes_category(restype)))
+    assert not bad, bad
