@@ -54,9 +54,10 @@ INT_MAD_PEAK_T = 18.85
 FP64_FMA_PEAK_T = 0.504
 FP32_FMA_PEAK_T = 35.9
 # dram__bytes_read.sum + dram__bytes_write.sum per launch divided by the amplitudes of
-# the captured case (profiles/k_window_tma_fp64_24q_full.md: 479.9 MB at 2^24;
-# profiles/k_window_phases_c64_26q_full.md: 1012.3 MB at 2^26;
-# profiles/k_window_tc_24q_full.md: 476.1 MB at 2^24).
+# the captured case: one ncu capture per kernel on a smaller state of the same ladder
+# workload (k_window_tma<PolF64>: 479.9 MB at 2^24 amplitudes; k_window_phases<PolF32>:
+# 1012.3 MB at 2^26; k_window_tc: 476.1 MB at 2^24). Traffic is the state read plus
+# written once per pass, so it scales with the number of amplitudes.
 NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 479.873280e6 / (1 << 24),
                              ("window", "c64"): 1012.291328e6 / (1 << 26),
                              ("window", "c128", "tc"): 476.122112e6 / (1 << 24)}
@@ -168,11 +169,23 @@ def max_over_ranks(world, x: float) -> float:
 
 
 # ------------------------------------------------------------------ reference
+def workloads_standalone():
+    """damavand_gb300/workloads.py loaded by file path, outside the package: importing the
+    package maps libdamavand_gpu.so, which the CPU reference arm must not load."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("dmv_workloads_standalone",
+                                                  os.path.join(REPO, "damavand_gb300", "workloads.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def run_reference(args, world, rank):
     """CPU oracle (port of the reference's multithreading path) on the host cores."""
     if rank != 0:
         return None
-    from damavand_gb300.workloads import count, ladder_circuit
+    wl = workloads_standalone()
+    count, ladder_circuit = wl.count, wl.ladder_circuit
     from oracle import oracle
     oracle.build()
     n = args.qubits
@@ -283,11 +296,26 @@ def adjoint_section(args):
     t_ps_per_param = (time.perf_counter() - t0) / k
     c.set_parameters(p)
     t_ps = t_ps_per_param * p.size
-    return {"qubits": n, "params": int(p.size), "gates": len(gates), "adjoint_s": t_adj,
-            "adjoint_grads_per_s": p.size / t_adj, "param_shift_s_extrapolated": t_ps,
-            "param_shift_grads_per_s": p.size / t_ps, "param_shift_sampled_params": int(k),
-            "speedup_vs_param_shift": t_ps / t_adj, "max_abs_diff_vs_param_shift": float(np.max(np.abs(g[idx] - ps))),
-            "loss": loss}
+    out = {"qubits": n, "params": int(p.size), "gates": len(gates), "adjoint_s": t_adj,
+           "adjoint_grads_per_s": p.size / t_adj, "param_shift_s_extrapolated": t_ps,
+           "param_shift_grads_per_s": p.size / t_ps, "param_shift_sampled_params": int(k),
+           "speedup_vs_param_shift": t_ps / t_adj, "max_abs_diff_vs_param_shift": float(np.max(np.abs(g[idx] - ps))),
+           "loss": loss}
+    if not args.no_cpu:
+        # The reference has no gradient; its route is parameter shift (circuit.rs:529-546):
+        # two CPU forwards (clone per gate) per parameter. One loss evaluation timed here.
+        from oracle import oracle
+        oracle.build()
+        og = [(kk, t, cc, int(o), th) for kk, t, cc, o, th in gates]
+        t0 = time.perf_counter()
+        oracle.loss(n, og, p, w, clone=True)
+        t_loss = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / (2.0 * t_loss), "unit": "grads/s", "cores": oracle.num_threads(),
+                               "kind": "port", "extrapolated": True,
+                               "sample": f"one oracle loss evaluation ({n} qubits, {len(gates)} gates, clone per gate: "
+                                         f"{t_loss:.1f} s); parameter shift needs two per parameter, "
+                                         f"{2 * t_loss * p.size:.0f} s for all {p.size}"}
+    return out
 
 
 def normwise_err(got, ref, chunk: int = 1 << 26) -> float:
@@ -311,38 +339,125 @@ def batch_section(args):
     gates_total = sum(count(g) for _, g in circuits)
     amps = sum(1 << n for n, _ in circuits)
     out, ez = {}, {}
-    for prec, size in (("complex128", 16), ("complex64", 8)):
-        b = Batch(circuits, prec)
+    runs = [("complex128", "fp64", 16), ("complex128", "fp32x2", 16), ("complex128", "int64", 16),
+            ("complex64", "fp32", 8)]
+    for prec, arith, size in runs:
+        b = Batch(circuits, prec, "fp64" if prec == "complex64" else arith)
         tune = b.autotune()
         b.run()
-        times = [b.run() for _ in range(max(3, args.steps))]
+        times = [b.run() for _ in range(max(3, min(args.steps, 5)))]
         ms = float(np.median(times))
         st = b.stats()
-        out[prec] = {"ms_per_run": ms, "circuits_per_s": len(circuits) / (ms / 1e3),
-                     "gate_applies_per_s": gates_total / (ms / 1e3), "autotuned": tune, "items": st["items"],
-                     "passes": st["passes"], "grid": st["grid"], "cuda_graph": st["cuda_graph"],
-                     "arena_gb": amps * size / 1e9}
-        ez[prec] = b.expect_z()
+        key = prec if arith in ("fp64", "fp32") else f"{prec}_{arith}"
+        out[key] = {"arithmetic": arith, "ms_per_run": ms, "circuits_per_s": len(circuits) / (ms / 1e3),
+                    "gate_applies_per_s": gates_total / (ms / 1e3), "autotuned": tune, "items": st["items"],
+                    "passes": st["passes"], "grid": st["grid"], "cuda_graph": st["cuda_graph"],
+                    "arena_gb": amps * size / 1e9}
+        ez[key] = b.expect_z()
         del b
-    err = [float(np.max(np.abs(a - b))) for a, b in zip(ez["complex64"], ez["complex128"])]
-    out["complex64_expect_z_err_vs_complex128"] = {"max": max(err), "median": float(np.median(err))}
+    for key in ez:
+        if key == "complex128":
+            continue
+        err = [float(np.max(np.abs(a - b))) for a, b in zip(ez[key], ez["complex128"])]
+        out[key]["expect_z_err_vs_complex128_fp64"] = {"max": max(err), "median": float(np.median(err))}
+    out["complex64_expect_z_err_vs_complex128"] = out["complex64"]["expect_z_err_vs_complex128_fp64"]
     out["circuits"] = len(circuits)
     out["gates"] = gates_total
+    if not args.no_cpu:
+        # The reference runs one circuit per process: the oracle (clone per gate) over the
+        # circuits in order, for about cpu_seconds, scaled to the batch.
+        from oracle import oracle
+        oracle.build()
+        done, g_done, t0 = 0, 0, time.perf_counter()
+        while done < len(circuits) and time.perf_counter() - t0 < args.cpu_seconds:
+            nq, gates = circuits[done]
+            oracle.forward(nq, [(kk, t, cc, int(o), th) for kk, t, cc, o, th in gates], clone=True)
+            g_done += count(gates)
+            done += 1
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": done / el, "unit": "circuits/s", "cores": oracle.num_threads(),
+                               "kind": "port", "gate_applies_per_s": g_done / el,
+                               "sample": f"the first {done} of the {len(circuits)} circuits ({g_done} gates, {el:.1f} s)"}
+    return out
+
+
+def config1_section(args):
+    """The 20-qubit configuration end to end through the Circuit API: H on every qubit + 10 x
+    [RX, RY, RZ per qubit; CNOT i->i+1] (seed 0, 810 gates), forward, measure (2^20
+    probabilities to the host), 1000 samples and the per-qubit <Z> (readout observables),
+    against the same pipeline in the oracle (clone per gate, the sampler rebuilding its
+    cumulative sum for every sample as sample_from_discrete_distribution does)."""
+    import torch
+
+    from damavand_gb300 import Circuit
+    from damavand_gb300.workloads import add_to_circuit, count, ladder_circuit
+    n = 20
+    gates = ladder_circuit(n, 10, seed=0)
+    u = np.random.default_rng([0, 1]).random(1000)
+    c = Circuit(n)
+    add_to_circuit(c, gates)
+
+    def run():
+        c.reset_amplitudes()
+        c.forward()
+        probs = c.probabilities()
+        samples = c.sample_array(1000, uniforms=u)
+        ev = np.asarray(c.extract_expectation_values(samples)).mean(axis=0)
+        return probs, samples, ev
+
+    for _ in range(3):
+        run()
+    reps = 10
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        probs, samples, ev = run()
+    t_gpu = (time.perf_counter() - t0) / reps
+    out = {"qubits": n, "gates": count(gates), "samples": 1000, "seconds_per_run": t_gpu,
+           "runs_per_s": 1.0 / t_gpu, "gate_applies_per_s": count(gates) / t_gpu,
+           "pipeline": "forward + measure (probabilities to host) + 1000 samples + extract_expectation_values"}
+    if not args.no_cpu:
+        from oracle import oracle
+        oracle.build()
+        og = [(kk, t, cc, int(o), th) for kk, t, cc, o, th in gates]
+        t0 = time.perf_counter()
+        st = oracle.forward(n, og, clone=True)
+        t_fwd = time.perf_counter() - t0
+        p = oracle.measure(st)
+        t1 = time.perf_counter()
+        s_ref = oracle.sample(p, u, rebuild_per_sample=True)
+        t_smp = time.perf_counter() - t1
+        oracle.extract_expectation_values(s_ref, list(range(n)))
+        t_cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "runs/s", "cores": oracle.num_threads(), "kind": "port",
+                               "sample": f"the whole pipeline once: forward {t_fwd:.2f} s, 1000 samples with the "
+                                         f"per-sample cumulative sum {t_smp:.2f} s, total {t_cpu:.2f} s"}
+        out["speedup_vs_cpu_baseline"] = t_cpu / t_gpu
+        out["samples_equal_oracle"] = int(np.sum(np.asarray(samples, dtype=np.uint64) == s_ref))
+        out["probabilities_normwise_err_vs_oracle"] = float(np.max(np.abs(probs - p)) / np.max(p))
+    del c
+    torch.cuda.empty_cache()
     return out
 
 
 def large_section(args):
-    """31 qubits complex128: forward + adjoint of the 12-layer ring ansatz (1116 parameters, seed 5,
-    loss = mean <Z_i>); 32 qubits complex64 forward with FP64 reductions, compared with complex128."""
+    """The large-state configuration. 31 qubits complex128 (three 34.4 GB statevectors for the
+    adjoint): forward + adjoint of the 12-layer ring ansatz (1116 parameters, seed 5, loss =
+    mean <Z_i>), two sampled gradients checked against parameter shift through the same GPU
+    kernels. 32 qubits complex64 (34.4 GB) forward with FP64 reductions; its error is reported
+    against complex128 (FP64 arithmetic) on the 30-qubit prefix of the same circuit (its gates
+    on qubits 0..29, same angles), run in both precisions."""
     import torch
 
     from damavand_gb300 import Circuit
-    from damavand_gb300.workloads import add_to_circuit, ring_ansatz
+    from damavand_gb300.workloads import add_to_circuit, parameters, ring_ansatz
     res = {}
     n = 31
     gates = ring_ansatz(n, 12, seed=5)
     c = Circuit(n)
     add_to_circuit(c, gates)
+    c.forward()  # warm-up (plans, tensor maps, first-touch of the 34.4 GB state)
+    c.reset_amplitudes()
+    c.synchronize()
     t0 = time.perf_counter()
     c.forward()
     c.synchronize()
@@ -355,27 +470,53 @@ def large_section(args):
     res["adjoint31_params"] = int(grads.size)
     res["adjoint31_grads_per_s"] = grads.size / res["adjoint31_s"]
     res["adjoint31_loss"] = loss
+    p = parameters(gates)
+    which = [0, p.size - 1]
+    diffs = []
+    for j in which:
+        up, dn = p.copy(), p.copy()
+        up[j] += math.pi / 2
+        dn[j] -= math.pi / 2
+        c.set_parameters(up)
+        lu = c.loss(w)
+        c.set_parameters(dn)
+        ld = c.loss(w)
+        diffs.append(abs(0.5 * (lu - ld) - grads[j]))
+    c.set_parameters(p)
+    res["adjoint31_check"] = {"against": "parameter shift through the same GPU kernels", "params": which,
+                              "max_abs_diff": float(max(diffs)), "tolerance": 1e-10, "ok": max(diffs) <= 1e-10}
     del c
     torch.cuda.empty_cache()
+
     m = 32
     g32 = ring_ansatz(m, 12, seed=5)
     c64 = Circuit(m, precision="complex64")
     add_to_circuit(c64, g32)
+    c64.forward()
+    c64.reset_amplitudes()
+    c64.synchronize()
     t0 = time.perf_counter()
     c64.forward()
     c64.synchronize()
     res["forward32_c64_s"] = time.perf_counter() - t0
     res["forward32_c64_gate_applies_per_s"] = len(g32) / res["forward32_c64_s"]
-    ez64 = c64.expectation_z()
-    c128 = Circuit(m, arithmetic="fp32x2")
-    add_to_circuit(c128, g32)
-    c128.forward()
-    ez128 = c128.expectation_z()
-    res["c64_vs_c128_32q_expect_z_max_err"] = float(np.max(np.abs(ez64 - ez128)))
-    a, b = c64.state().torch(), c128.state().torch()
-    res["c64_vs_c128_32q_amp_normwise_err"] = normwise_err(a, b)
-    res["c128_32q_reference_arithmetic"] = "fp32x2 (9e-14 from FP64 at 30 qubits)"
-    del a, b, c64, c128
+    ez = c64.expectation_z()
+    res["forward32_c64_norm"] = float(c64.norm())
+    res["forward32_c64_mean_abs_expect_z"] = float(np.mean(np.abs(ez)))
+    del c64
+    torch.cuda.empty_cache()
+    prefix = [g for g in g32 if g[1] < 30 and g[2] < 30]
+    a = Circuit(30, precision="complex64")
+    b = Circuit(30)  # complex128, FP64 arithmetic
+    for cc in (a, b):
+        add_to_circuit(cc, prefix)
+        cc.forward()
+    res["c64_vs_c128_prefix30"] = {
+        "gates": len(prefix),
+        "expect_z_max_abs_err": float(np.max(np.abs(a.expectation_z() - b.expectation_z()))),
+        "amplitude_normwise_err": normwise_err(a.state().torch(), b.state().torch()),
+        "against": "complex128 (FP64 arithmetic) forward of the 32-qubit circuit's gates on qubits 0..29"}
+    del a, b
     torch.cuda.empty_cache()
     return res
 
@@ -393,18 +534,21 @@ def read_families(lib, check):
     return fam
 
 
-def timed_forward(c, args, world, local):
-    """W warm-up steps, then K steps between CUDA events on the library's stream (profiled)."""
+def timed_forward(c, args, world, local, steps=None, warmup=None):
+    """W warm-up steps, then K steps between CUDA events on the library's stream (profiled).
+    The headline uses the command line's K and W; the secondary lines pass fewer."""
     import ctypes
 
     from damavand_gb300._lib import check, lib
     st = c.state()
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
 
     def step():
         c.reset_amplitudes()
         c.forward()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     st.synchronize()
     barrier(world)
@@ -414,14 +558,14 @@ def timed_forward(c, args, world, local):
     launches0 = lib.dmv_kernel_launch_count()
     with ClockSampler(local) as clocks:
         check(lib.dmv_state_event_begin(st.handle))
-        for _ in range(args.steps):
+        for _ in range(steps):
             step()
         ms = ctypes.c_double()
         check(lib.dmv_state_event_end(st.handle, ctypes.byref(ms)))
     launches = lib.dmv_kernel_launch_count() - launches0
     lib.dmv_profile_enable(0)
     barrier(world)
-    step_ms = max_over_ranks(world, ms.value / args.steps)
+    step_ms = max_over_ranks(world, ms.value / steps)
     return step_ms, read_families(lib, check), launches, clocks.summary(), step
 
 
@@ -442,7 +586,7 @@ def rooflines(fam, n, arith, prec="c128"):
     per_launch_bytes = d["bytes"] / max(d["launches"], 1)
     avg_launch_s = d["ms"] / max(d["launches"], 1) / 1e3
     achieved = per_launch_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
-    # DRAM bytes per launch from one ncu capture (profiles/*_full.md), scaled by state size.
+    # DRAM bytes per launch from one ncu capture of the same kernel, scaled by state size.
     traffic = None
     key = (dom, prec, arith) if (dom, prec, arith) in NCU_TRAFFIC_PER_AMPLITUDE else (dom, prec)
     if key in NCU_TRAFFIC_PER_AMPLITUDE:
@@ -576,12 +720,15 @@ def run_ours(args, world, rank, local):
     # ---- the other complex128 arithmetics, same workload and protocol, each checked against FP64
     if not args.no_alt:
         import torch
+        # secondary lines: fewer steps than the headline (each is reported with its own count)
+        sec_steps, sec_warmup = max(1, min(args.steps, 5)), min(args.warmup, 3)
         alts = [a for a in ("fp64", "fp32x2", "int64", "tc") if a != args.arith]
         out["alt_arithmetic"] = []
         for alt in alts:
             c2 = Circuit(n, "gpu", fusion=not args.no_fusion, arithmetic=alt)
             add_to_circuit(c2, gates)
-            ms2, fam2, launches2, clocks2, _ = timed_forward(c2, args, world, local)
+            ms2, fam2, launches2, clocks2, _ = timed_forward(c2, args, world, local, steps=sec_steps,
+                                                             warmup=sec_warmup)
             rl2, ra2, gbs2 = rooflines(fam2, n, alt)
             ta, tb = c2.state().torch(), c.state().torch()  # both hold one forward from |0...0>
             if args.arith == "fp64":
@@ -594,7 +741,7 @@ def run_ours(args, world, rank, local):
             del ta, tb, ref, other
             entry = {
                 "arithmetic": alt, "dtype": DTYPES[alt], "value": world * G / (ms2 / 1e3), "unit": UNIT,
-                "ms_per_step": ms2, "roofline": rl2, "roofline_arith": ra2, "hbm_gbs_pass_bytes": gbs2,
+                "ms_per_step": ms2, "steps": sec_steps, "warmup": sec_warmup, "roofline": rl2, "roofline_arith": ra2, "hbm_gbs_pass_bytes": gbs2,
                 "gpu_launches": int(launches2), "clocks": clocks2}
             if alt == "tc":
                 entry["tensor_core_passes"] = tc_stats(c2)
@@ -609,12 +756,13 @@ def run_ours(args, world, rank, local):
         # complex128 state.
         c3 = Circuit(n, "gpu", fusion=not args.no_fusion, precision="complex64")
         add_to_circuit(c3, gates)
-        ms3, fam3, launches3, clocks3, _ = timed_forward(c3, args, world, local)
+        ms3, fam3, launches3, clocks3, _ = timed_forward(c3, args, world, local, steps=sec_steps,
+                                                         warmup=sec_warmup)
         rl3, ra3, gbs3 = rooflines(fam3, n, "fp32", prec="c64")
         err = normwise_err(c3.state().torch(), c.state().torch())
         out["complex64"] = {
             "dtype": "c64 (complex64 storage, FP32 arithmetic)", "value": world * G / (ms3 / 1e3), "unit": UNIT,
-            "ms_per_step": ms3, "roofline": rl3, "roofline_arith": ra3, "hbm_gbs_pass_bytes": gbs3,
+            "ms_per_step": ms3, "steps": sec_steps, "warmup": sec_warmup, "roofline": rl3, "roofline_arith": ra3, "hbm_gbs_pass_bytes": gbs3,
             "gpu_launches": int(launches3), "clocks": clocks3,
             "error": {"against": f"the {args.arith} complex128 forward of this run", "normwise_max_err": err}}
         del c3
@@ -623,10 +771,16 @@ def run_ours(args, world, rank, local):
         out["adjoint"] = adjoint_section(args)
     if rank == 0 and not args.no_batch:
         out["batch"] = batch_section(args)
-    if rank == 0 and args.workload == "large":
+    if rank == 0 and not args.no_config1:
+        out["config1"] = config1_section(args)
+    if rank == 0 and not args.no_large:
         out["large"] = large_section(args)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
+        if "complex64" in out:
+            # the reference has complex128 only: the same CPU forward is the baseline of the c64 line
+            out["complex64"]["cpu_baseline"] = dict(out["cpu_baseline"], note="the reference's complex128 CPU "
+                                                    "forward of the same workload (it has no complex64 path)")
     return out
 
 
@@ -646,8 +800,10 @@ def main():
                          "int64 block fixed point, or the same with dense blocks on the tensor cores")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--workload", choices=["default", "large"], default="default",
-                    help="'large' adds the 31-qubit forward + adjoint and the 32-qubit complex64 forward")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 31-qubit forward + adjoint and the 32-qubit complex64 forward")
+    ap.add_argument("--no-config1", action="store_true",
+                    help="skip the 20-qubit forward + measure + 1000 samples pipeline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-gates", type=int, default=3, help="gates per reference step")

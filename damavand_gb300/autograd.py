@@ -2,11 +2,20 @@
 
 ``circuit_loss(circuit, params, weights)`` returns
 L = sum_q w_q <Z_q> of the circuit run from |0...0> with its RX/RY/RZ angles
-set to ``params`` (Circuit.set_parameters order). Its backward uses the
-adjoint sweep of libdamavand_gpu (one forward plus one reverse pass that
+set to ``params`` (Circuit.set_parameters order). The forward runs the
+circuit and the exact <Z_q> reduction only. The gradient with respect to the
+angles is computed in ``backward``, and only when autograd asks for it, by the
+adjoint sweep of libdamavand_gpu: one forward plus one reverse pass that
 uncomputes the state, with the per-parameter Im<lambda|P|psi> reductions
-fused into the sweep) instead of 2P parameter-shift forwards. dL/dw_q is the
-exact <Z_q>.
+fused into the sweep, instead of 2P parameter-shift forwards. dL/dw_q is the
+exact <Z_q> saved by the forward.
+
+Tensors may live on any device; results come back on the device (and in the
+dtype) of the tensor they belong to. The angles always cross to the host once
+per call: the gate matrices are formed on the host with the same libm calls as
+the reference's gate formulas (src/qubit_backend/gates.rs), so that every
+arithmetic starts from identical coefficients. <Z_q> (n values) and the
+gradients (one per angle) come back from the library as host arrays.
 """
 from __future__ import annotations
 
@@ -17,26 +26,31 @@ import torch
 class CircuitExpectation(torch.autograd.Function):
     @staticmethod
     def forward(ctx, params: torch.Tensor, weights: torch.Tensor, circuit):
-        p = params.detach().to("cpu", torch.float64).numpy()
-        w = weights.detach().to("cpu", torch.float64).numpy()
+        p = params.detach().to("cpu", torch.float64).numpy().copy()
         circuit.set_parameters(p)
-        if params.requires_grad:
-            loss, grads = circuit.adjoint_gradient(w)
-        else:
-            loss, grads = circuit.loss(w), np.zeros(p.size)
-        ez = circuit.expectation_z()  # state holds the forward state in both branches
-        ctx.save_for_backward(torch.from_numpy(np.asarray(grads, dtype=np.float64)),
-                              torch.from_numpy(np.asarray(ez, dtype=np.float64)))
-        ctx.devices = (params.device, weights.device)
-        ctx.dtypes = (params.dtype, weights.dtype)
-        return torch.tensor(loss, dtype=params.dtype, device=params.device)
+        circuit.reset_amplitudes()
+        circuit.forward()
+        ez = torch.from_numpy(np.asarray(circuit.expectation_z(), dtype=np.float64)).to(weights.device)
+        loss = torch.dot(weights.detach().to(torch.float64), ez)
+        ctx.circuit = circuit
+        ctx.params = p
+        ctx.save_for_backward(weights.detach(), ez)
+        ctx.param_meta = (params.device, params.dtype)
+        return loss.to(device=params.device, dtype=params.dtype)
 
     @staticmethod
     def backward(ctx, grad_out):
-        grads, ez = ctx.saved_tensors
-        g = grad_out.detach().to("cpu", torch.float64)
-        gp = (g * grads).to(ctx.devices[0], ctx.dtypes[0])
-        gw = (g * ez).to(ctx.devices[1], ctx.dtypes[1])
+        weights, ez = ctx.saved_tensors
+        gp = gw = None
+        if ctx.needs_input_grad[0]:
+            w = weights.to("cpu", torch.float64).numpy()
+            ctx.circuit.set_parameters(ctx.params)
+            _, grads = ctx.circuit.adjoint_gradient(w)
+            dev, dt = ctx.param_meta
+            g = torch.from_numpy(np.asarray(grads, dtype=np.float64)).to(dev)
+            gp = (grad_out.detach().to(dev, torch.float64) * g).to(dt)
+        if ctx.needs_input_grad[1]:
+            gw = (grad_out.detach().to(ez.device, torch.float64) * ez).to(weights.dtype)
         return gp, gw, None
 
 

@@ -2,11 +2,11 @@
 //
 // dmv_expect_z computes its per-CTA partial sums in device buffers that the
 // library allocates (and keeps) on the state. Some callers cannot let a
-// library allocate: a CUDA graph being captured forbids cudaMalloc, a serving
-// process may hand out all device memory from its own pool up front, and
-// cudaMalloc/cudaFree synchronise the device, which a latency-bound loop
-// cannot afford. dmv_expect_z_noalloc performs the same reduction with its
-// scratch in a fixed-size array compiled into this library instead.
+// library allocate: a serving process may hand out all device memory from
+// its own pool up front, and cudaMalloc/cudaFree synchronise the device,
+// which a latency-bound loop cannot afford. dmv_expect_z_noalloc performs
+// the same reduction with its scratch in a fixed-size array compiled into
+// this library instead.
 //
 // The scratch is a file-scope __device__ array: every GPU that loads the
 // library holds it (332.5 KiB) until the process exits. Host code must not
@@ -28,6 +28,10 @@ namespace {
 constexpr int kNaThreads = 256;
 constexpr int kNaChunkBits = 13;     // 8192 amplitudes per chunk
 constexpr int kNaRows = 32;          // (1 << kNaChunkBits) / kNaThreads
+constexpr int kNaTotalThread = kNaThreads - 1;  // writes the CTA's total mass
+static_assert((1 << kNaChunkBits) == kNaThreads * kNaRows, "a chunk is one element per thread and row");
+static_assert(kNaThreads == 256 && kNaRows == 32, "bits 0-7 of an element index come from the thread, 8-12 from the row");
+static_assert(kNaChunkBits < kNaTotalThread, "the total's thread must not be one of the per-bit threads");
 constexpr int kNaMaxQubits = 34;
 constexpr int kNaMaxCtas = 1216;     // grid cap, fixed so the scratch bound holds on any GPU
 constexpr int kNaScratchDoubles = kNaMaxCtas * (kNaMaxQubits + 1);  // 42,560 doubles
@@ -113,7 +117,7 @@ k_expect_z_noalloc(const V* __restrict__ a, int n, int chunk_bits, int64_t num_c
       for (int t = 0; t < kNaThreads; ++t) acc += rsum[q - 8][t];
     }
     out[q] = acc;
-  } else if (q == 64) {
+  } else if (q == kNaTotalThread) {
     double acc = 0.;
     for (int t = 0; t < kNaThreads; ++t) acc += tsum[t];
     out[n] = acc;

@@ -217,10 +217,10 @@ int dmv_sample_expect_z(dmv_state_t s, const double* uniforms, uint64_t seed, in
 int dmv_inner_product(dmv_state_t a, dmv_state_t b, double* re, double* im);
 
 /* Allocation-free <Z_q> for callers that must not let a library allocate
- * device memory: code being captured into a CUDA graph (cudaMalloc is not
- * allowed there), applications that hand all device memory out from their
- * own pool, and loops that cannot take the device-wide synchronisation of
- * cudaMalloc/cudaFree. It has no counterpart in the reference.
+ * device memory: applications that hand all device memory out from their
+ * own pool up front, and latency-bound loops that cannot take the
+ * device-wide synchronisation of cudaMalloc/cudaFree. It has no counterpart
+ * in the reference.
  * `amps` are the caller's 2^num_qubits device amplitudes (interleaved, in
  * `precision`); `out_device` receives num_qubits + 1 doubles on the device:
  * <Z_0> ... <Z_{n-1}>, then the norm. Stream-ordered on `stream`. It calls

@@ -94,19 +94,64 @@ void orc_apply_gate(double* state, double* scratch, int32_t n, const double m[8]
   }
 }
 
-/* Circuit::forward, src/qubit_backend/circuit.rs:341-369: observables skipped. */
-void orc_forward(double* state, int32_t n, const orc_gate* gates, int64_t num_gates) {
+/* The same update as orc_apply_gate without the clone: every amplitude pair
+ * (i, i + 2^target) with bit `target` of i clear is read once and both
+ * outputs are written in place. Each output is the expression of
+ * circuit_multithreading.rs:46-49 on the same two inputs, in the same order
+ * of operations (a*m00 + partner*m01 for the lower index, partner*m10 +
+ * a*m11 for the upper), so the result is bit-identical to orc_apply_gate:
+ * the clone only guarantees that every read sees the pre-gate values, which
+ * reading each pair before writing it guarantees as well. The control is
+ * tested on the lower index; both indices of a pair share every bit but
+ * `target` (control != target). */
+void orc_apply_gate_inplace(double* state, int32_t n, const double m[8], int32_t control,
+                            int32_t target) {
+  int64_t half = (int64_t)1 << (n - 1);
+  int64_t gap = (int64_t)1 << target;
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < half; ++j) {
+    int64_t i = ((j >> target) << (target + 1)) | (j & (gap - 1)); /* bit `target` clear */
+    if (control >= 0 && !((i >> control) & 1)) continue;
+    int64_t p = i + gap;
+    double ar = state[2 * i], ai = state[2 * i + 1];
+    double pr = state[2 * p], pi = state[2 * p + 1];
+    double t0r, t0i, t1r, t1i, u0r, u0i, u1r, u1i;
+    cmul(ar, ai, m[0], m[1], &t0r, &t0i); /* lower: a*m00 + partner*m01 */
+    cmul(pr, pi, m[2], m[3], &t1r, &t1i);
+    cmul(ar, ai, m[4], m[5], &u0r, &u0i); /* upper: partner*m10 + a*m11 */
+    cmul(pr, pi, m[6], m[7], &u1r, &u1i);
+    state[2 * i] = t0r + t1r;
+    state[2 * i + 1] = t0i + t1i;
+    state[2 * p] = u0r + u1r;
+    state[2 * p + 1] = u0i + u1i;
+  }
+}
+
+/* Circuit::forward, src/qubit_backend/circuit.rs:341-369: observables skipped.
+ * clone_per_gate = 1 runs orc_apply_gate (the reference's clone and sweep, the
+ * algorithm the CPU baseline times); 0 runs orc_apply_gate_inplace (same
+ * bits, half the memory traffic and no scratch vector). */
+void orc_forward_mode(double* state, int32_t n, const orc_gate* gates, int64_t num_gates,
+                      int32_t clone_per_gate) {
   int64_t N = (int64_t)1 << n;
-  double* scratch = (double*)malloc((size_t)N * 2 * sizeof(double));
-  if (!scratch) return;
+  double* scratch = NULL;
+  if (clone_per_gate) {
+    scratch = (double*)malloc((size_t)N * 2 * sizeof(double));
+    if (!scratch) return;
+  }
   for (int64_t g = 0; g < num_gates; ++g) {
     if (gates[g].is_observable) continue;
     double m[8];
     orc_gate_matrix(gates[g].kind, gates[g].theta, m);
     int32_t control = gates[g].kind == ORC_CNOT ? gates[g].control : -1;
-    orc_apply_gate(state, scratch, n, m, control, gates[g].target);
+    if (clone_per_gate) orc_apply_gate(state, scratch, n, m, control, gates[g].target);
+    else orc_apply_gate_inplace(state, n, m, control, gates[g].target);
   }
   free(scratch);
+}
+
+void orc_forward(double* state, int32_t n, const orc_gate* gates, int64_t num_gates) {
+  orc_forward_mode(state, n, gates, num_gates, 1);
 }
 
 /* Circuit::measure CPU branch, src/qubit_backend/circuit.rs:579-581 (norm_sqr). */
@@ -168,6 +213,32 @@ void orc_expect_z(const double* probs, int32_t n, double* out) {
   }
 }
 
+/* The same <Z_q> straight from the amplitudes (p_i = norm_sqr, circuit.rs:579-581)
+ * in one pass, for states whose probability vector would not fit beside them. */
+void orc_expect_z_from_state(const double* state, int32_t n, double* out) {
+  int64_t N = (int64_t)1 << n;
+  double total = 0.;
+  for (int32_t q = 0; q < n; ++q) out[q] = 0.;
+#pragma omp parallel
+  {
+    double set[64] = {0.};
+    double tot = 0.;
+#pragma omp for schedule(static) nowait
+    for (int64_t i = 0; i < N; ++i) {
+      double p = state[2 * i] * state[2 * i] + state[2 * i + 1] * state[2 * i + 1];
+      tot += p;
+      for (int32_t q = 0; q < n; ++q)
+        if ((i >> q) & 1) set[q] += p;
+    }
+#pragma omp critical
+    {
+      total += tot;
+      for (int32_t q = 0; q < n; ++q) out[q] += set[q];
+    }
+  }
+  for (int32_t q = 0; q < n; ++q) out[q] = total - 2. * out[q];
+}
+
 /* Circuit::extract_expectation_values, src/qubit_backend/circuit.rs:494-513. */
 void orc_extract_expectation_values(const uint64_t* samples, int64_t k,
                                     const int32_t* readout_qubits, int32_t num_obs,
@@ -181,8 +252,8 @@ static int is_parametrised(int32_t kind) {
   return kind == ORC_RX || kind == ORC_RY || kind == ORC_RZ;
 }
 
-double orc_loss(int32_t n, const orc_gate* gates, int64_t num_gates,
-                const double* params, int64_t num_params, const double* weights) {
+double orc_loss_mode(int32_t n, const orc_gate* gates, int64_t num_gates, const double* params,
+                     int64_t num_params, const double* weights, int32_t clone_per_gate) {
   int64_t N = (int64_t)1 << n;
   orc_gate* g = (orc_gate*)malloc((size_t)num_gates * sizeof(orc_gate));
   double* state = (double*)malloc((size_t)N * 2 * sizeof(double));
@@ -196,7 +267,7 @@ double orc_loss(int32_t n, const orc_gate* gates, int64_t num_gates,
     for (int64_t i = 0; i < num_gates && p < num_params; ++i)
       if (is_parametrised(g[i].kind)) g[i].theta = params[p++];
     orc_zero_state(state, n);
-    orc_forward(state, n, g, num_gates);
+    orc_forward_mode(state, n, g, num_gates, clone_per_gate);
     orc_measure(state, n, probs);
     orc_expect_z(probs, n, ez);
     loss = 0.;
@@ -204,6 +275,33 @@ double orc_loss(int32_t n, const orc_gate* gates, int64_t num_gates,
   }
   free(g); free(state); free(probs); free(ez);
   return loss;
+}
+
+double orc_loss(int32_t n, const orc_gate* gates, int64_t num_gates,
+                const double* params, int64_t num_params, const double* weights) {
+  return orc_loss_mode(n, gates, num_gates, params, num_params, weights, 1);
+}
+
+/* Parameter shift for the parameters listed in `which` (num_which of them):
+ * grads[j] = (L(th_k + pi/2) - L(th_k - pi/2)) / 2 for k = which[j]. */
+void orc_param_shift_subset(int32_t n, const orc_gate* gates, int64_t num_gates,
+                            const double* params, int64_t num_params, const double* weights,
+                            const int64_t* which, int64_t num_which, double* grads,
+                            int32_t clone_per_gate) {
+  const double half_pi = 1.5707963267948966;
+  double* shifted = (double*)malloc((size_t)num_params * sizeof(double));
+  if (!shifted) return;
+  memcpy(shifted, params, (size_t)num_params * sizeof(double));
+  for (int64_t j = 0; j < num_which; ++j) {
+    int64_t k = which[j];
+    shifted[k] = params[k] + half_pi;
+    double up = orc_loss_mode(n, gates, num_gates, shifted, num_params, weights, clone_per_gate);
+    shifted[k] = params[k] - half_pi;
+    double down = orc_loss_mode(n, gates, num_gates, shifted, num_params, weights, clone_per_gate);
+    shifted[k] = params[k];
+    grads[j] = 0.5 * (up - down);
+  }
+  free(shifted);
 }
 
 void orc_param_shift_grad(int32_t n, const orc_gate* gates, int64_t num_gates,

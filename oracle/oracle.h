@@ -54,8 +54,18 @@ void orc_zero_state(double* state, int32_t n);
 void orc_apply_gate(double* state, double* scratch, int32_t n, const double m[8],
                     int32_t control, int32_t target);
 
-/* Circuit::forward: every non-observable gate in order. Does NOT reset. */
+/* The same gate in place over amplitude pairs, without the clone; each output
+ * is the reference's expression on the same inputs, so the bits are those of
+ * orc_apply_gate (checked by the oracle tests). */
+void orc_apply_gate_inplace(double* state, int32_t n, const double m[8], int32_t control,
+                            int32_t target);
+
+/* Circuit::forward: every non-observable gate in order. Does NOT reset.
+ * orc_forward clones per gate (the reference's algorithm); orc_forward_mode
+ * with clone_per_gate = 0 uses orc_apply_gate_inplace. */
 void orc_forward(double* state, int32_t n, const orc_gate* gates, int64_t num_gates);
+void orc_forward_mode(double* state, int32_t n, const orc_gate* gates, int64_t num_gates,
+                      int32_t clone_per_gate);
 
 /* Circuit::measure on the CPU path: norm_sqr of every amplitude. */
 void orc_measure(const double* state, int32_t n, double* probs);
@@ -76,6 +86,9 @@ void orc_sample(const double* probs, int64_t num_probs, const double* uniforms,
  * Circuit::extract_expectation_values). */
 void orc_expect_z(const double* probs, int32_t n, double* out);
 
+/* The same from the amplitudes, without a probability vector (n <= 64). */
+void orc_expect_z_from_state(const double* state, int32_t n, double* out);
+
 /* Circuit::extract_expectation_values: out[s*num_obs+j] = -1 if bit
  * readout[j] of samples[s] is set, else +1. */
 void orc_extract_expectation_values(const uint64_t* samples, int64_t k,
@@ -86,6 +99,15 @@ void orc_extract_expectation_values(const uint64_t* samples, int64_t k,
  * angles replaced in gate order by `params` (Circuit::set_parameters). */
 double orc_loss(int32_t n, const orc_gate* gates, int64_t num_gates,
                 const double* params, int64_t num_params, const double* weights);
+
+double orc_loss_mode(int32_t n, const orc_gate* gates, int64_t num_gates, const double* params,
+                     int64_t num_params, const double* weights, int32_t clone_per_gate);
+
+/* Parameter shift for the parameters with indices which[0..num_which). */
+void orc_param_shift_subset(int32_t n, const orc_gate* gates, int64_t num_gates,
+                            const double* params, int64_t num_params, const double* weights,
+                            const int64_t* which, int64_t num_which, double* grads,
+                            int32_t clone_per_gate);
 
 /* Parameter-shift gradient of orc_loss: g_k = (L(th_k + pi/2) - L(th_k - pi/2))/2,
  * the rule sketched (commented out) at src/qubit_backend/circuit.rs:529-546. */

@@ -50,17 +50,27 @@ def lib():
         L.orc_zero_state.argtypes = [dp, ctypes.c_int32]
         L.orc_apply_gate.argtypes = [dp, dp, ctypes.c_int32, dp, ctypes.c_int32, ctypes.c_int32]
         L.orc_forward.argtypes = [dp, ctypes.c_int32, ctypes.POINTER(OrcGate), ctypes.c_int64]
+        L.orc_forward_mode.argtypes = [dp, ctypes.c_int32, ctypes.POINTER(OrcGate), ctypes.c_int64,
+                                       ctypes.c_int32]
+        L.orc_apply_gate_inplace.argtypes = [dp, ctypes.c_int32, dp, ctypes.c_int32, ctypes.c_int32]
         L.orc_measure.argtypes = [dp, ctypes.c_int32, dp]
         L.orc_sample_one.argtypes = [dp, ctypes.c_int64, ctypes.c_double]
         L.orc_sample_one.restype = ctypes.c_uint64
         L.orc_sample.argtypes = [dp, ctypes.c_int64, dp, ctypes.c_int64,
                                  ctypes.POINTER(ctypes.c_uint64), ctypes.c_int32]
         L.orc_expect_z.argtypes = [dp, ctypes.c_int32, dp]
+        L.orc_expect_z_from_state.argtypes = [dp, ctypes.c_int32, dp]
         L.orc_extract_expectation_values.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_int64,
                                                      ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, dp]
         L.orc_loss.argtypes = [ctypes.c_int32, ctypes.POINTER(OrcGate), ctypes.c_int64, dp,
                                ctypes.c_int64, dp]
         L.orc_loss.restype = ctypes.c_double
+        L.orc_loss_mode.argtypes = [ctypes.c_int32, ctypes.POINTER(OrcGate), ctypes.c_int64, dp,
+                                    ctypes.c_int64, dp, ctypes.c_int32]
+        L.orc_loss_mode.restype = ctypes.c_double
+        L.orc_param_shift_subset.argtypes = [ctypes.c_int32, ctypes.POINTER(OrcGate), ctypes.c_int64, dp,
+                                             ctypes.c_int64, dp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int64,
+                                             dp, ctypes.c_int32]
         L.orc_param_shift_grad.argtypes = [ctypes.c_int32, ctypes.POINTER(OrcGate), ctypes.c_int64,
                                            dp, ctypes.c_int64, dp, dp]
         L.orc_num_threads.restype = ctypes.c_int32
@@ -94,13 +104,24 @@ def zero_state(n: int) -> np.ndarray:
     return s
 
 
-def forward(n: int, gates, state: np.ndarray | None = None) -> np.ndarray:
-    """Run the circuit on `state` (default |0...0>) in place; returns it."""
+def forward(n: int, gates, state: np.ndarray | None = None, clone: bool = True) -> np.ndarray:
+    """Run the circuit on `state` (default |0...0>) in place; returns it.
+
+    clone=True clones the state for every gate, as the reference does (the
+    algorithm the CPU baseline times); clone=False updates amplitude pairs in
+    place with the same expressions, bit-identical, with half the memory
+    traffic and no second statevector (for the large parity checks)."""
     if state is None:
         state = zero_state(n)
     assert state.dtype == np.complex128 and state.flags.c_contiguous and state.size == 1 << n
     arr, ng = gates_array(gates)
-    lib().orc_forward(_dp(state.view(np.float64)), n, arr, ng)
+    lib().orc_forward_mode(_dp(state.view(np.float64)), n, arr, ng, int(bool(clone)))
+    return state
+
+
+def apply_gate_inplace(state: np.ndarray, n: int, m: np.ndarray, control: int, target: int) -> np.ndarray:
+    mm = np.ascontiguousarray(np.stack([m.real, m.imag], axis=-1).reshape(-1))
+    lib().orc_apply_gate_inplace(_dp(state.view(np.float64)), n, _dp(mm), control, target)
     return state
 
 
@@ -140,6 +161,14 @@ def expect_z(probs: np.ndarray) -> np.ndarray:
     return out
 
 
+def expect_z_from_state(state: np.ndarray) -> np.ndarray:
+    """<Z_q> from complex128 amplitudes in one pass (no probability vector)."""
+    n = int(state.size).bit_length() - 1
+    out = np.empty(n)
+    lib().orc_expect_z_from_state(_dp(np.ascontiguousarray(state).view(np.float64)), n, _dp(out))
+    return out
+
+
 def extract_expectation_values(samples: np.ndarray, readout_qubits) -> np.ndarray:
     s = np.ascontiguousarray(samples, dtype=np.uint64)
     q = np.ascontiguousarray(readout_qubits, dtype=np.int32)
@@ -150,11 +179,25 @@ def extract_expectation_values(samples: np.ndarray, readout_qubits) -> np.ndarra
     return out
 
 
-def loss(n: int, gates, params: np.ndarray, weights: np.ndarray) -> float:
+def loss(n: int, gates, params: np.ndarray, weights: np.ndarray, clone: bool = True) -> float:
     arr, ng = gates_array(gates)
     p = np.ascontiguousarray(params, dtype=np.float64)
     w = np.ascontiguousarray(weights, dtype=np.float64)
-    return float(lib().orc_loss(n, arr, ng, _dp(p), p.size, _dp(w)))
+    return float(lib().orc_loss_mode(n, arr, ng, _dp(p), p.size, _dp(w), int(bool(clone))))
+
+
+def param_shift_subset(n: int, gates, params: np.ndarray, weights: np.ndarray, which,
+                       clone: bool = True) -> np.ndarray:
+    """Parameter-shift gradient (src/qubit_backend/circuit.rs:529-546 rule) of the listed parameters."""
+    arr, ng = gates_array(gates)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    idx = np.ascontiguousarray(which, dtype=np.int64)
+    g = np.empty(idx.size)
+    lib().orc_param_shift_subset(n, arr, ng, _dp(p), p.size, _dp(w),
+                                 idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), idx.size, _dp(g),
+                                 int(bool(clone)))
+    return g
 
 
 def param_shift_grad(n: int, gates, params: np.ndarray, weights: np.ndarray) -> np.ndarray:

@@ -94,3 +94,47 @@ def test_autograd_function(built_lib, oracle_mod):
     assert np.max(np.abs(pt.grad.numpy() - ps)) < GRAD_ATOL
     ez = oracle_mod.expect_z(oracle_mod.measure(oracle_mod.forward(n, og)))
     assert np.max(np.abs(wt.grad.numpy() - ez)) < 1e-12
+
+
+def _adjoint_launches(lib):
+    import ctypes
+
+    from damavand_gb300._lib import KERNEL_ADJOINT, check
+    l, t, b, fm = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    check(lib.dmv_profile_read(KERNEL_ADJOINT, ctypes.byref(l), ctypes.byref(t), ctypes.byref(b), ctypes.byref(fm)))
+    return l.value
+
+
+def test_autograd_forward_runs_no_sweep_and_keeps_device_tensors(built_lib, oracle_mod):
+    """The loss alone runs no adjoint kernel; backward does, and the gradients land on
+    the device (and in the dtype) of the tensors they belong to."""
+    torch = pytest.importorskip("torch")
+    from damavand_gb300 import Circuit
+    from damavand_gb300._lib import lib
+    from damavand_gb300.autograd import circuit_loss
+    from damavand_gb300.workloads import add_to_circuit
+    n = 6
+    gates, params, w = _ansatz(n, 2, seed=60)
+    c = Circuit(n)
+    add_to_circuit(c, gates)
+    pt = torch.tensor(params, dtype=torch.float64, device="cuda", requires_grad=True)
+    wt = torch.tensor(w, dtype=torch.float32, device="cuda", requires_grad=True)
+    lib.dmv_profile_reset()
+    lib.dmv_profile_enable(1)
+    try:
+        L = circuit_loss(c, pt, wt)
+        assert L.device.type == "cuda"
+        assert _adjoint_launches(lib) == 0
+        L.backward()
+        assert _adjoint_launches(lib) > 0
+    finally:
+        lib.dmv_profile_enable(0)
+    og = [(k, t, cc, int(o), th) for k, t, cc, o, th in gates]
+    w32 = wt.detach().cpu().numpy().astype(np.float64)
+    ps = oracle_mod.param_shift_grad(n, og, params, w32)
+    assert pt.grad.device.type == "cuda" and pt.grad.dtype == torch.float64
+    assert np.max(np.abs(pt.grad.cpu().numpy() - ps)) < GRAD_ATOL
+    assert wt.grad.device.type == "cuda" and wt.grad.dtype == torch.float32
+    ez = oracle_mod.expect_z(oracle_mod.measure(oracle_mod.forward(n, og)))
+    assert np.max(np.abs(wt.grad.cpu().numpy() - ez)) < 1e-6  # float32 gradient
+    assert abs(L.item() - oracle_mod.loss(n, og, params, w32)) < 1e-12

@@ -124,3 +124,51 @@ def test_oracle_forward_does_not_reset(oracle_mod):
     st = oracle_mod.forward(1, [(1, 0, -1, 0, 0.0)])
     st = oracle_mod.forward(1, [(1, 0, -1, 0, 0.0)], st)
     np.testing.assert_array_equal(st, np.array([1, 0], dtype=np.complex128))
+
+
+def test_oracle_inplace_update_is_bit_identical_to_the_clone(oracle_mod, built_lib):
+    """The in-place pair update (used for the 30- and 31-qubit parity checks) gives the
+    same bits as the reference's clone-and-sweep restatement, for every gate kind,
+    controlled and not, on every target."""
+    from damavand_gb300.workloads import ladder_circuit, random_circuit, ring_ansatz
+    rng = np.random.default_rng(77)
+    n = 9
+    circuits = [random_circuit(n, 6, rng), ring_ansatz(n, 2, seed=3), ladder_circuit(n, 2, seed=4)]
+    for gates in circuits:
+        og = [(k, t, c, int(o), th) for k, t, c, o, th in gates]
+        a = oracle_mod.forward(n, og, clone=True)
+        b = oracle_mod.forward(n, og, clone=False)
+        assert np.array_equal(a.view(np.float64), b.view(np.float64))
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    m = oracle_mod.gate_matrix(5, 0.7) @ oracle_mod.gate_matrix(0)
+    for control in (-1, 0, 4, 8):
+        for target in range(n):
+            if target == control:
+                continue
+            a = oracle_mod.apply_gate(psi.copy(), n, m, control, target)
+            b = oracle_mod.apply_gate_inplace(psi.copy(), n, m, control, target)
+            assert np.array_equal(a.view(np.float64), b.view(np.float64)), (control, target)
+
+
+def test_oracle_param_shift_subset_matches_full(oracle_mod, built_lib):
+    from damavand_gb300.workloads import loss_weights, parameters, ring_ansatz
+    n = 4
+    gates = ring_ansatz(n, 2, seed=9)
+    og = [(k, t, c, int(o), th) for k, t, c, o, th in gates]
+    p, w = parameters(gates), loss_weights(n, 10)
+    full = oracle_mod.param_shift_grad(n, og, p, w)
+    which = [0, 5, p.size - 1]
+    for clone in (True, False):
+        sub = oracle_mod.param_shift_subset(n, og, p, w, which, clone=clone)
+        # the OpenMP reduction in orc_expect_z combines thread partials in no fixed order
+        assert np.max(np.abs(sub - full[which])) < 1e-15
+
+
+def test_oracle_expect_z_from_state_matches_probabilities(oracle_mod):
+    rng = np.random.default_rng(12)
+    n = 13
+    v = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    v /= np.linalg.norm(v)
+    a = oracle_mod.expect_z(oracle_mod.measure(v))
+    b = oracle_mod.expect_z_from_state(v)
+    assert np.max(np.abs(a - b)) < 1e-14
