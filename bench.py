@@ -42,7 +42,10 @@ sys.path.insert(0, REPO)
 
 METRIC = "30-qubit gate applies/s + HBM GB/s; adjoint vs param-shift grads/s at 1e-10"
 UNIT = "gate-applies/s"
-DTYPES = {"fp64": "f64 (complex128 storage and FP64 arithmetic)",
+DTYPES = {"fp64": "f64 (complex128 storage, IEEE FP64 arithmetic; fused passes as real rotations applied as "
+                  "three shears and per-amplitude phase tables)",
+          "fp64-direct": "f64 (complex128 storage, IEEE FP64 arithmetic; every fused 2x2 as a full complex "
+                         "multiply-add)",
           "fp32x2": "f32x2 (complex128 storage, FP32-pair arithmetic, ~48-bit)",
           "int64": "int64 (complex128 storage, block fixed point: 54-bit fraction per tile, exact products)",
           "tc": "int64 (complex128 storage, block fixed point: 56-bit fraction per tile; fused gates as dense "
@@ -62,7 +65,8 @@ NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 479.873280e6 / (1 << 24),
                              ("window", "c64"): 1012.291328e6 / (1 << 26),
                              ("window", "c128", "tc"): 476.122112e6 / (1 << 24)}
 # The kernel that runs a fused window pass, by arithmetic and precision.
-WINDOW_KERNEL = {("fp64", "c128"): "k_window_tma<PolF64>", ("fp32x2", "c128"): "k_apply_window<PolDF>",
+WINDOW_KERNEL = {("fp64", "c128"): "k_window_tma<PolF64>", ("fp64-direct", "c128"): "k_window_tma<PolF64>",
+                 ("fp32x2", "c128"): "k_apply_window<PolDF>",
                  ("int64", "c128"): "k_apply_window<PolFX>", ("tc", "c128"): "k_window_tc",
                  ("fp32", "c64"): "k_window_phases<PolF32>"}
 
@@ -484,7 +488,7 @@ def large_section(args):
         diffs.append(abs(0.5 * (lu - ld) - grads[j]))
     c.set_parameters(p)
     res["adjoint31_check"] = {"against": "parameter shift through the same GPU kernels", "params": which,
-                              "max_abs_diff": float(max(diffs)), "tolerance": 1e-10, "ok": max(diffs) <= 1e-10}
+                              "max_abs_diff": float(max(diffs)), "tolerance": 1e-10, "ok": bool(max(diffs) <= 1e-10)}
     del c
     torch.cuda.empty_cache()
 
@@ -598,7 +602,7 @@ def rooflines(fam, n, arith, prec="c128"):
     # The same kernel against the arithmetic ceiling it meets on GB300: FP64
     # multiply-adds for IEEE FP64 arithmetic, FP32 operations for FP32-pair arithmetic.
     rate = d["arith_ops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else 0.0
-    if arith == "fp64":
+    if arith in ("fp64", "fp64-direct"):
         ra = {"bound": "fp64", "achieved": rate, "peak": FP64_FMA_PEAK_T, "unit": "T FMA/s",
               "frac": rate / FP64_FMA_PEAK_T, "peak_source": "measured (FP64 FMA chain kernel on this pool's GB300)"}
     elif arith == "tc":
@@ -648,7 +652,9 @@ def run_ours(args, world, rank, local):
     for a in (pin_params, re, im):
         if lib.dmv_host_register(a.ctypes.data, a.nbytes) == 0:
             registered.append(a)
-    h2d = pin_params.nbytes + G * ctypes.sizeof(ctypes.c_double) * 20  # parameters + uploaded op list
+    up_total, up_tab = ctypes.c_int64(), ctypes.c_int64()
+    check(lib.dmv_last_upload_bytes(st.handle, ctypes.byref(up_total), ctypes.byref(up_tab)))
+    h2d = pin_params.nbytes + up_total.value  # parameters + the plan's op list and phase tables
     d2h = re.nbytes + im.nbytes
     c.set_parameters(pin_params)
     step()
@@ -676,7 +682,8 @@ def run_ours(args, world, rank, local):
         "roofline": roofline,
         "roofline_arith": roofline_arith,
         "e2e": {"value": world * G / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                "h2d_phase_table_bytes": int(up_tab.value)},
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
@@ -722,7 +729,7 @@ def run_ours(args, world, rank, local):
         import torch
         # secondary lines: fewer steps than the headline (each is reported with its own count)
         sec_steps, sec_warmup = max(1, min(args.steps, 5)), min(args.warmup, 3)
-        alts = [a for a in ("fp64", "fp32x2", "int64", "tc") if a != args.arith]
+        alts = [a for a in ("fp64", "fp64-direct", "fp32x2", "int64", "tc") if a != args.arith]
         out["alt_arithmetic"] = []
         for alt in alts:
             c2 = Circuit(n, "gpu", fusion=not args.no_fusion, arithmetic=alt)
@@ -747,7 +754,7 @@ def run_ours(args, world, rank, local):
                 entry["tensor_core_passes"] = tc_stats(c2)
             if err is not None:
                 entry["parity"] = {"against": "the FP64-arithmetic forward of this run", "normwise_max_err": err,
-                                   "tolerance": 1e-12, "ok": err <= 1e-12}
+                                   "tolerance": 1e-12, "ok": bool(err <= 1e-12)}
             out["alt_arithmetic"].append(entry)
             del c2
             torch.cuda.empty_cache()
@@ -795,8 +802,9 @@ def main():
     ap.add_argument("--no-fusion", action="store_true")
     ap.add_argument("--no-alt", action="store_true",
                     help="skip the other complex128 arithmetics (timed and checked against FP64)")
-    ap.add_argument("--arith", choices=["fp64", "fp32x2", "int64", "tc"], default="fp64",
-                    help="complex128 arithmetic: IEEE FP64, FP32 pairs (error-free transformations), "
+    ap.add_argument("--arith", choices=["fp64", "fp64-direct", "fp32x2", "int64", "tc"], default="fp64",
+                    help="complex128 arithmetic: IEEE FP64 (rotations as shears and phase tables, or every 2x2 "
+                         "as a full complex multiply-add), FP32 pairs (error-free transformations), "
                          "int64 block fixed point, or the same with dense blocks on the tensor cores")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
@@ -815,7 +823,7 @@ def main():
     else:
         out = run_ours(args, world, rank, local)
     if rank == 0 and out is not None:
-        print(json.dumps(out))
+        print(json.dumps(out, default=lambda o: o.item() if hasattr(o, "item") else str(o)))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -17,7 +17,7 @@ OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_NO_DEVICE, ERR_UNSUPPORTED, ERR_TIMEOUT,
 C128, C64 = 0, 1
 GATE_H, GATE_X, GATE_Y, GATE_Z, GATE_RX, GATE_RY, GATE_RZ, GATE_CNOT, GATE_MATRIX = range(9)
 FUSE_NONE, FUSE_WINDOW = 0, 1
-ARITH_FP64, ARITH_FP32X2, ARITH_INT64, ARITH_TC = 0, 1, 2, 3
+ARITH_FP64, ARITH_FP32X2, ARITH_INT64, ARITH_TC, ARITH_FP64_DIRECT = 0, 1, 2, 3, 4
 KERNEL_WINDOW, KERNEL_SINGLE, KERNEL_REDUCE, KERNEL_ADJOINT, KERNEL_OTHER = range(5)
 
 _ERROR_NAMES = {ERR_INVALID: "invalid argument", ERR_OOM: "out of memory", ERR_CUDA: "CUDA error",
@@ -76,6 +76,7 @@ SIGNATURES = {
     "dmv_apply_gates": (ctypes.c_int, [_vp, ctypes.POINTER(Gate), _i64, _i32]),
     "dmv_last_plan_stats": (ctypes.c_int, [_i64p, _i64p, _i64p]),
     "dmv_last_tc_stats": (ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),
+    "dmv_last_upload_bytes": (ctypes.c_int, [_vp, _i64p, _i64p]),
     "dmv_plan_describe": (ctypes.c_int, [_i32, _i32, ctypes.POINTER(Gate), _i64, _i32, _i32, _i64p, _i64p, _i64p,
                                          _i32p]),
     "dmv_measure": (ctypes.c_int, [_vp, _dp]),
@@ -99,6 +100,7 @@ SIGNATURES = {
     "dmv_debug_fail_allocations": (ctypes.c_int, [_i32]),
     "dmv_debug_tma_wait_limit": (ctypes.c_int, [_i64]),
     "dmv_debug_tc_convert": (ctypes.c_int, [_i32]),
+    "dmv_debug_check_fp64_rewrite": (ctypes.c_int, [ctypes.c_void_p, _i64, _i32, ctypes.c_uint64, _dp, _i64p]),
     "dmv_circuit_create": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, _vpp]),
     "dmv_circuit_destroy": (ctypes.c_int, [_vp]),
     "dmv_circuit_add_gate": (ctypes.c_int, [_vp, _i32, _i32, _i32, _f64, _i32]),

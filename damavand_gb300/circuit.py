@@ -89,13 +89,14 @@ class Circuit:
         self.set_arithmetic(arithmetic)
 
     def set_arithmetic(self, arithmetic: str) -> None:
-        """Arithmetic on the complex128 amplitudes (complex64 ignores it): 'fp64' (IEEE FP64
-        multiply-adds), 'fp32x2' (FP32-pair error-free arithmetic, ~1e-13 normwise on deep
-        circuits), 'int64' (block fixed point with exact integer products) or 'tc' (the same
-        block fixed point, fused gates applied as dense 5-qubit blocks by exact digit products
-        on the tensor cores)."""
-        modes = {"fp64": _lib.ARITH_FP64, "fp32x2": _lib.ARITH_FP32X2, "int64": _lib.ARITH_INT64,
-                 "tc": _lib.ARITH_TC}
+        """Arithmetic on the complex128 amplitudes (complex64 ignores it): 'fp64' (IEEE FP64;
+        fused passes apply rotations and phase tables as shears), 'fp64-direct' (IEEE FP64,
+        every fused 2x2 as a full complex multiply-add), 'fp32x2' (FP32-pair error-free
+        arithmetic, ~1e-13 normwise on deep circuits), 'int64' (block fixed point with exact
+        integer products) or 'tc' (the same block fixed point, fused gates applied as dense
+        5-qubit blocks by exact digit products on the tensor cores)."""
+        modes = {"fp64": _lib.ARITH_FP64, "fp64-direct": _lib.ARITH_FP64_DIRECT, "fp32x2": _lib.ARITH_FP32X2,
+                 "int64": _lib.ARITH_INT64, "tc": _lib.ARITH_TC}
         if arithmetic not in modes:
             raise ValueError(f"arithmetic must be one of {sorted(modes)}")
         check(lib.dmv_circuit_set_arithmetic(self._h, modes[arithmetic]))

@@ -452,9 +452,10 @@ extern "C" int dmv_state_set_arithmetic(dmv_state_t s, int32_t arithmetic) {
   clear_error();
   DMV_TRY(check_state(s));
   if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2 && arithmetic != DMV_ARITH_INT64 &&
-      arithmetic != DMV_ARITH_TC)
+      arithmetic != DMV_ARITH_TC && arithmetic != DMV_ARITH_FP64_DIRECT)
     return set_error(DMV_ERR_INVALID, "unknown arithmetic %d", arithmetic);
-  s->arith = arithmetic;
+  s->arith = arithmetic == DMV_ARITH_FP64_DIRECT ? (int32_t)dmv::ARITH_FP64 : arithmetic;
+  s->fp64_rewrite = arithmetic == DMV_ARITH_FP64;
   return DMV_OK;
 }
 
@@ -607,6 +608,14 @@ extern "C" int dmv_plan_describe(int32_t num_qubits, int32_t precision, const dm
   if (num_window_passes) *num_window_passes = windows;
   if (num_ops) *num_ops = (int64_t)plan.ops.size();
   if (max_local_qubits) *max_local_qubits = max_local;
+  return DMV_OK;
+}
+
+extern "C" int dmv_last_upload_bytes(dmv_state_t s, int64_t* total, int64_t* phase_tables) {
+  clear_error();
+  DMV_TRY(check_state(s));
+  if (total) *total = s->last_upload_bytes;
+  if (phase_tables) *phase_tables = s->last_phase_tab_bytes;
   return DMV_OK;
 }
 
@@ -1042,7 +1051,7 @@ void legacy_flush(const char* where) {
 }
 
 // Complex128 arithmetic of the legacy state: DAMAVAND_GB300_ARITHMETIC = fp64
-// (default), fp32x2, int64 or tc, so an unchanged front-end can select it.
+// (default), fp64-direct, fp32x2, int64 or tc, so an unchanged front-end can select it.
 int32_t legacy_arithmetic() {
   const char* v = std::getenv("DAMAVAND_GB300_ARITHMETIC");
   if (!v || !*v) return DMV_ARITH_FP64;
@@ -1050,6 +1059,7 @@ int32_t legacy_arithmetic() {
   if (a == "fp32x2") return DMV_ARITH_FP32X2;
   if (a == "int64") return DMV_ARITH_INT64;
   if (a == "tc") return DMV_ARITH_TC;
+  if (a == "fp64-direct") return DMV_ARITH_FP64_DIRECT;
   if (a != "fp64") std::fprintf(stderr, "damavand_gb300: unknown DAMAVAND_GB300_ARITHMETIC '%s': fp64\n", v);
   return DMV_ARITH_FP64;
 }

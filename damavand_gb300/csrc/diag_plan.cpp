@@ -1,0 +1,435 @@
+// Fewer FP64 operations for FP64 window passes (host C++).
+//
+// On GB300 a complex128 window pass in IEEE FP64 is bound by the FP64
+// multiply-add rate, not by HBM: a general 2x2 costs 8 multiply-adds per
+// amplitude. The rewrite here spends fewer of them on the same unitary:
+//
+//  * An uncontrolled unitary U = [[a, b], [c, d]] is written as
+//    U = D1 R D2 with R = [[cos t, -sin t], [sin t, cos t]] (t in [0, pi/2],
+//    cos t = |a|, sin t = |b|), D2 = diag(1, e^{i g}) and
+//    D1 = diag(e^{i arg a}, e^{i arg c}), g = arg b + pi - arg a. The
+//    product is checked against U entry by entry; an op it does not
+//    reproduce to 4e-15 stays as it was. R acts on the real parts and the
+//    imaginary parts of a pair as the same real rotation, and a rotation is
+//    three shears, x0 += T x1, x1 += S x0, x0 += T x1 (T = -tan(t/2),
+//    S = sin t): 3 multiply-adds per amplitude instead of 8.
+//  * Diagonal factors are not applied where they occur. Each is a phase per
+//    amplitude that depends on a few tile bits. Moving a diagonal later in
+//    time past an exchange (X, CNOT: a permutation P of the tile) re-indexes
+//    it, D then P = P then D o P; past an op whose target is not one of its
+//    bits it commutes. Moving it earlier past such ops also commutes. So the
+//    factors collect into tables of one phase per amplitude, applied as one
+//    op ("flush") where a rotation needs a bit the pending table depends on,
+//    and at the end of the pass. A factor whose bits nothing has touched
+//    since the last table joins that table instead of the pending one. An
+//    exchange controlled from outside the tile re-indexes only the tiles
+//    whose control bit is 1, so a table may depend on up to three global
+//    bits (then it holds 2^(k+g) phases and each tile reads its slice).
+//  * A table's phase phi becomes i^q e^{i phi'} with |phi'| <= pi/4: the
+//    kernel rotates (re, im) by phi' with three shears (3 multiply-adds) and
+//    multiplies by i^q with a swap and sign flips on the integer pipe.
+//
+// On the 30-qubit ladder forward (600 fused single-qubit unitaries in 85
+// passes) this takes the FP64 work from 4800 to about 2650 multiply-adds
+// per amplitude (600 rotations and about 284 tables).
+#include <cmath>
+#include <algorithm>
+#include <cstring>
+
+#include "internal.h"
+
+namespace dmv {
+namespace {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr double kHalfPi = 1.5707963267948966192313216916398;
+constexpr double kZyzTol = 4e-15;  // per entry, about 18 ulp of 1
+
+inline double wrap(double a) { return std::remainder(a, kTwoPi); }
+
+// A diagonal phase over the tile (2^k amplitudes) and up to kMaxPhaseGlobals
+// global bits: angle of amplitude l on tiles with global-bit pattern gsel at
+// index (gsel << k) | l.
+struct DiagTable {
+  int g = 0;
+  int gq[kMaxPhaseGlobals] = {0, 0, 0};
+  uint32_t supp = 0;  // local bits it depends on
+  bool used = false;
+  std::vector<double> ang;
+  void reset(int T) {
+    g = 0;
+    supp = 0;
+    used = false;
+    ang.assign((size_t)T, 0.0);
+  }
+};
+
+// Adds the phase f(l) of one diagonal factor (local bits only) to every slice.
+template <typename F>
+void add_term(DiagTable& d, int k, uint32_t bits, F f) {
+  const size_t T = size_t(1) << k;
+  for (size_t idx = 0; idx < d.ang.size(); ++idx) {
+    const double a = f((uint32_t)(idx & (T - 1)));
+    if (a != 0.0) d.ang[idx] = wrap(d.ang[idx] + a);
+  }
+  d.supp |= bits;
+  d.used = true;
+}
+
+// D o P for the exchange `op` (X or CNOT on tile bit op.target). Returns false,
+// changing nothing, when the table would need a fourth global bit.
+bool permute(DiagTable& d, int k, const Op& op) {
+  const uint32_t tb = 1u << op.target;
+  if (!(d.supp & tb)) return true;  // does not depend on the target: unchanged
+  const size_t T = size_t(1) << k;
+  std::vector<double> old = d.ang;
+  if (op.ctrl_kind == CTRL_NONE) {
+    for (size_t idx = 0; idx < old.size(); ++idx) d.ang[idx] = old[idx ^ tb];
+  } else if (op.ctrl_kind == CTRL_LOCAL) {
+    const int c = op.ctrl;
+    for (size_t idx = 0; idx < old.size(); ++idx) d.ang[idx] = old[idx ^ (((idx >> c) & 1u) ? tb : 0u)];
+    d.supp |= 1u << c;
+  } else {
+    int j = -1;
+    for (int i = 0; i < d.g; ++i)
+      if (d.gq[i] == op.ctrl) j = i;
+    if (j < 0) {
+      if (d.g == kMaxPhaseGlobals) return false;
+      j = d.g++;
+      d.gq[j] = op.ctrl;
+      d.ang.resize(old.size() * 2);
+      std::memcpy(d.ang.data() + old.size(), old.data(), old.size() * sizeof(double));
+      old = d.ang;
+    }
+    for (size_t idx = 0; idx < old.size(); ++idx) {
+      const bool on = ((idx >> k) >> j) & 1u;
+      d.ang[idx] = on ? old[idx ^ tb] : old[idx];
+    }
+    (void)T;
+  }
+  return true;
+}
+
+inline double cabs(double re, double im) { return std::hypot(re, im); }
+
+// U = D1 R D2 (see the file comment). Returns false when the product does not
+// reproduce U to kZyzTol in every entry.
+bool zyz(const double m[8], double& T, double& S, double& a1, double& a2, double& g2) {
+  const double ra = cabs(m[0], m[1]), rb = cabs(m[2], m[3]);
+  const double r = std::hypot(ra, rb);
+  if (!(r > 0.0)) return false;
+  const double c = ra / r, s = rb / r;
+  a1 = std::atan2(m[1], m[0]);
+  a2 = std::atan2(m[5], m[4]);
+  g2 = wrap(std::atan2(m[3], m[2]) + M_PI - a1);
+  const double e[8] = {c * std::cos(a1),        c * std::sin(a1),
+                       -s * std::cos(a1 + g2),  -s * std::sin(a1 + g2),
+                       s * std::cos(a2),        s * std::sin(a2),
+                       c * std::cos(a2 + g2),   c * std::sin(a2 + g2)};
+  for (int i = 0; i < 8; ++i)
+    if (!(std::fabs(e[i] - m[i]) <= kZyzTol)) return false;
+  T = -s / (1.0 + c);  // -tan(t/2), t = atan2(s, c) in [0, pi/2]
+  S = s;
+  return true;
+}
+
+// |z| = 1 to kZyzTol: a diagonal entry that is a pure phase.
+inline bool unit(double re, double im) { return std::fabs(cabs(re, im) - 1.0) <= kZyzTol; }
+
+PhaseEntry entry_of(double phi) {
+  // phi = q pi/2 + phi', |phi'| <= pi/4
+  const double qf = std::nearbyint(phi / kHalfPi);
+  const double p = phi - qf * kHalfPi;
+  const int q = (((int)qf % 4) + 4) % 4;
+  PhaseEntry e;
+  const double h = 0.5 * p;
+  e.t = -std::tan(h);
+  e.s = std::sin(p);
+  e.swap_xy = (uint32_t)(q & 1);
+  e.sign_x = (q == 1 || q == 2) ? 0x80000000u : 0u;
+  e.sign_y = (q == 2 || q == 3) ? 0x80000000u : 0u;
+  e.pad = 0;
+  return e;
+}
+
+struct Item {
+  bool flush;   // a table (index `table`) rather than `op`
+  int table;
+  Op op;
+};
+
+Op blank_op() {
+  Op o;
+  std::memset(&o, 0, sizeof(o));
+  o.param = -1;
+  o.unitary = 1;
+  return o;
+}
+
+}  // namespace
+
+int64_t rewrite_pass_fp64(const Op* src, int64_t count, int32_t k, std::vector<Op>& dst,
+                          std::vector<PhaseEntry>& tab) {
+  const int T = 1 << k;
+  std::vector<DiagTable> tables;  // flushes in time order; tables[0] may sit at the pass start
+  bool start_table = false;
+  std::vector<Item> items;
+  int last = -1;          // table the next factor may join, -1: none yet
+  uint32_t touched = 0;   // target bits of the ops emitted after `last` (after the pass start if none)
+  DiagTable pend;
+  pend.reset(T);
+
+  auto flush = [&]() {
+    if (!pend.used) return;
+    tables.push_back(pend);
+    items.push_back(Item{true, (int)tables.size() - 1, Op()});
+    last = (int)tables.size() - 1;
+    touched = 0;
+    pend.reset(T);
+  };
+  // A diagonal factor on `bits` with phase f(l): into the last table when
+  // nothing emitted since touches its bits, else pending.
+  auto diag = [&](uint32_t bits, auto f) {
+    if (!(bits & touched)) {
+      if (last < 0) {
+        DiagTable d;
+        d.reset(T);
+        tables.insert(tables.begin(), d);
+        for (Item& it : items)
+          if (it.flush) ++it.table;
+        start_table = true;
+        last = 0;
+      }
+      add_term(tables[(size_t)last], k, bits, f);
+    } else {
+      add_term(pend, k, bits, f);
+    }
+  };
+  auto emit = [&](const Op& op) {
+    items.push_back(Item{false, -1, op});
+    touched |= 1u << op.target;
+  };
+
+  for (int64_t i = 0; i < count; ++i) {
+    const Op& op = src[i];
+    const uint32_t tb = 1u << op.target;
+    if (op.cls == OP_SWAP) {
+      if (!permute(pend, k, op)) {
+        flush();
+        permute(pend, k, op);
+      }
+      emit(op);
+      continue;
+    }
+    if (op.unitary && op.ctrl_kind == CTRL_NONE &&
+        (op.cls == OP_GENERAL || op.cls == OP_REAL || op.cls == OP_RXLIKE)) {
+      double Tq, Sq, a1, a2, g2;
+      if (zyz(op.m, Tq, Sq, a1, a2, g2)) {
+        const int t = op.target;
+        if (g2 != 0.0) diag(tb, [=](uint32_t l) { return ((l >> t) & 1u) ? g2 : 0.0; });  // D2
+        if (pend.supp & tb) flush();
+        Op r = blank_op();
+        r.cls = OP_ROT;
+        r.target = t;
+        r.ctrl = -1;
+        r.ctrl_kind = CTRL_NONE;
+        r.m[0] = Tq;
+        r.m[1] = Sq;
+        emit(r);
+        // D1: after the rotation on its own bit, so it cannot join an earlier table
+        add_term(pend, k, tb, [=](uint32_t l) { return ((l >> t) & 1u) ? a2 : a1; });
+        continue;
+      }
+    }
+    if (op.unitary && op.cls == OP_DIAG && unit(op.m[0], op.m[1]) && unit(op.m[6], op.m[7]) &&
+        op.ctrl_kind != CTRL_GLOBAL) {
+      const int t = op.target;
+      const double p0 = std::atan2(op.m[1], op.m[0]), p1 = std::atan2(op.m[7], op.m[6]);
+      if (op.ctrl_kind == CTRL_NONE) {
+        diag(tb, [=](uint32_t l) { return ((l >> t) & 1u) ? p1 : p0; });
+      } else {
+        const int c = op.ctrl;
+        diag(tb | (1u << c), [=](uint32_t l) { return ((l >> c) & 1u) ? (((l >> t) & 1u) ? p1 : p0) : 0.0; });
+      }
+      continue;
+    }
+    if (op.unitary && op.cls == OP_ANTI && op.ctrl_kind == CTRL_NONE && unit(op.m[2], op.m[3]) &&
+        unit(op.m[4], op.m[5])) {
+      // [[0, b], [c, 0]] = X diag(c, b)
+      const int t = op.target;
+      const double pc = std::atan2(op.m[5], op.m[4]), pb = std::atan2(op.m[3], op.m[2]);
+      diag(tb, [=](uint32_t l) { return ((l >> t) & 1u) ? pb : pc; });
+      Op x = blank_op();
+      x.cls = OP_SWAP;
+      x.target = t;
+      x.ctrl = -1;
+      x.ctrl_kind = CTRL_NONE;
+      x.m[2] = 1.0;
+      x.m[4] = 1.0;
+      if (!permute(pend, k, x)) {
+        flush();
+        permute(pend, k, x);
+      }
+      emit(x);
+      continue;
+    }
+    // Anything else runs as it is, after the pending factors on its target.
+    if (pend.supp & tb) flush();
+    emit(op);
+  }
+  flush();
+
+  const int64_t before = (int64_t)dst.size();
+  auto put_table = [&](const DiagTable& d) {
+    bool trivial = true;
+    for (double a : d.ang)
+      if (a != 0.0) {
+        trivial = false;
+        break;
+      }
+    if (trivial) return;
+    Op p = blank_op();
+    p.cls = OP_PHASE;
+    p.target = 0;
+    p.ctrl = -1;
+    p.ctrl_kind = CTRL_NONE;
+    p.fh[0] = (int32_t)tab.size();
+    p.fh[1] = d.g;
+    for (int j = 0; j < d.g; ++j) p.fh[2 + j] = d.gq[j];
+    tab.reserve(tab.size() + d.ang.size());
+    for (double a : d.ang) tab.push_back(entry_of(a));
+    dst.push_back(p);
+  };
+  if (start_table) put_table(tables[0]);
+  for (const Item& it : items) {
+    if (it.flush) put_table(tables[(size_t)it.table]);
+    else dst.push_back(it.op);
+  }
+  return (int64_t)dst.size() - before;
+}
+
+}  // namespace dmv
+
+// ---------------------------------------------------------------------------
+// Host check of the rewrite (dmv_debug_check_fp64_rewrite): both op lists of
+// every window pass applied to random tiles in host FP64, compared normwise.
+// ---------------------------------------------------------------------------
+namespace dmv {
+namespace {
+
+struct Cx {
+  double re, im;
+};
+
+void host_op(std::vector<Cx>& tile, int k, const Op& op, const std::vector<PhaseEntry>& tab, uint64_t base) {
+  const uint32_t T = 1u << k;
+  if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1u)) return;
+  if (op.cls == OP_PHASE) {
+    uint32_t gsel = 0;
+    for (int j = 0; j < op.fh[1]; ++j) gsel |= (uint32_t)((base >> op.fh[2 + j]) & 1u) << j;
+    for (uint32_t l = 0; l < T; ++l) {
+      const PhaseEntry& e = tab[(size_t)op.fh[0] + ((size_t)gsel << k) + l];
+      Cx v = tile[l];
+      const double x1 = std::fma(e.t, v.im, v.re);
+      const double y1 = std::fma(e.s, x1, v.im);
+      const double x2 = std::fma(e.t, y1, x1);
+      double ox = e.swap_xy ? y1 : x2, oy = e.swap_xy ? x2 : y1;
+      if (e.sign_x) ox = -ox;
+      if (e.sign_y) oy = -oy;
+      tile[l] = Cx{ox, oy};
+    }
+    return;
+  }
+  const uint32_t tb = 1u << op.target;
+  for (uint32_t l0 = 0; l0 < T; ++l0) {
+    if (l0 & tb) continue;
+    if (op.ctrl_kind == CTRL_LOCAL && !((l0 >> op.ctrl) & 1u)) continue;
+    const uint32_t l1 = l0 | tb;
+    Cx a0 = tile[l0], a1 = tile[l1];
+    if (op.cls == OP_ROT) {
+      const double Tq = op.m[0], Sq = op.m[1];
+      double x0 = a0.re, x1 = a1.re, y0 = a0.im, y1 = a1.im;
+      x0 = std::fma(Tq, x1, x0); y0 = std::fma(Tq, y1, y0);
+      x1 = std::fma(Sq, x0, x1); y1 = std::fma(Sq, y0, y1);
+      x0 = std::fma(Tq, x1, x0); y0 = std::fma(Tq, y1, y0);
+      tile[l0] = Cx{x0, y0};
+      tile[l1] = Cx{x1, y1};
+    } else {
+      const double* m = op.m;
+      tile[l0] = Cx{m[0] * a0.re - m[1] * a0.im + m[2] * a1.re - m[3] * a1.im,
+                    m[0] * a0.im + m[1] * a0.re + m[2] * a1.im + m[3] * a1.re};
+      tile[l1] = Cx{m[4] * a0.re - m[5] * a0.im + m[6] * a1.re - m[7] * a1.im,
+                    m[4] * a0.im + m[5] * a0.re + m[6] * a1.im + m[7] * a1.re};
+    }
+  }
+}
+
+}  // namespace
+}  // namespace dmv
+
+extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num_gates, int32_t num_qubits,
+                                            uint64_t seed, double* max_err, int64_t* counts) {
+  using namespace dmv;
+  clear_error();
+  if (num_qubits < 12 || num_qubits > 34 || !max_err)
+    return set_error(DMV_ERR_INVALID, "dmv_debug_check_fp64_rewrite: num_qubits %d outside [12, 34]", num_qubits);
+  std::vector<Gate> g;
+  DMV_TRY(parse_gates(gates, num_gates, num_qubits, g));
+  PlanOptions opt;
+  opt.fusion = DMV_FUSE_WINDOW;
+  opt.tile_bits = 12;
+  Plan plan;
+  DMV_TRY(build_plan(g, num_qubits, DMV_C128, opt, plan));
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 1;
+  auto rnd = [&]() {  // SplitMix64
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  double worst = 0.0;
+  int64_t n_rot = 0, n_phase = 0, n_general = 0, n_passes = 0;
+  for (const Pass& ps : plan.passes) {
+    if (ps.kind != 1) continue;
+    const int k = ps.low_bits + ps.num_high;
+    if (k != 12 || ps.num_high < 3) continue;
+    ++n_passes;
+    std::vector<Op> rw;
+    std::vector<PhaseEntry> tab;
+    rewrite_pass_fp64(plan.ops.data() + ps.op_begin, ps.op_count, k, rw, tab);
+    for (const Op& o : rw) {
+      n_rot += o.cls == OP_ROT;
+      n_phase += o.cls == OP_PHASE;
+    }
+    for (int64_t o = 0; o < ps.op_count; ++o) n_general += plan.ops[(size_t)(ps.op_begin + o)].cls != OP_SWAP;
+    // local bit j of the tile index sits at global qubit pos[j]
+    int pos[12];
+    for (int j = 0; j < ps.low_bits; ++j) pos[j] = j;
+    for (int j = 0; j < ps.num_high; ++j) pos[ps.low_bits + j] = ps.high[j];
+    for (int trial = 0; trial < 2; ++trial) {
+      uint64_t base = rnd() & ((num_qubits >= 64 ? ~0ull : (1ull << num_qubits) - 1));
+      for (int j = 0; j < k; ++j) base &= ~(1ull << pos[j]);
+      std::vector<Cx> a(size_t(1) << k), b;
+      for (Cx& v : a) v = Cx{((double)(rnd() >> 11) * 0x1.0p-53) - 0.5, ((double)(rnd() >> 11) * 0x1.0p-53) - 0.5};
+      b = a;
+      // the original ops index controls outside the tile by global qubit; the host
+      // emulation reads them from `base`, as the kernel does
+      for (int64_t o = 0; o < ps.op_count; ++o) host_op(a, k, plan.ops[(size_t)(ps.op_begin + o)], tab, base);
+      for (const Op& o : rw) host_op(b, k, o, tab, base);
+      double num = 0.0, den = 0.0;
+      for (size_t i = 0; i < a.size(); ++i) {
+        num = std::max(num, std::hypot(a[i].re - b[i].re, a[i].im - b[i].im));
+        den = std::max(den, std::hypot(a[i].re, a[i].im));
+      }
+      worst = std::max(worst, den > 0 ? num / den : num);
+    }
+  }
+  *max_err = worst;
+  if (counts) {
+    counts[0] = n_passes;
+    counts[1] = n_general;
+    counts[2] = n_rot;
+    counts[3] = n_phase;
+  }
+  return DMV_OK;
+}

@@ -60,7 +60,10 @@ enum OpClass : int32_t {
   OP_SWAP = 2,     // exactly [[0,1],[1,0]] (X, CNOT): a pure exchange
   OP_REAL = 3,     // all four entries real
   OP_ANTI = 4,     // m00 = m11 = 0 (Y and scaled exchanges)
-  OP_RXLIKE = 5    // m00, m11 real and m01, m10 imaginary (RX and its adjoint): 8 multiply-adds
+  OP_RXLIKE = 5,   // m00, m11 real and m01, m10 imaginary (RX and its adjoint): 8 multiply-adds
+  // Only in FP64 window passes rewritten by rewrite_pass_fp64 (diag_plan.cpp):
+  OP_ROT = 6,      // real rotation [[c, -s], [s, c]] as three shears: m[0] = -tan(theta/2), m[1] = sin(theta)
+  OP_PHASE = 7     // every amplitude times a phase from a table (PhaseEntry); fields below
 };
 
 // Control kinds inside a fused pass.
@@ -87,6 +90,24 @@ struct alignas(16) Op {
   int32_t phase;      // register phase of a fused op (kPhase* below), 0 elsewhere
 };
 static_assert(sizeof(Op) == 224, "Op layout");
+
+// An OP_PHASE op multiplies amplitude l of a tile (2^k amplitudes) by the
+// phase of table entry fh[0] + (gsel << k) + l, where gsel collects the
+// tile's bits at the fh[1] (at most 3) global qubits fh[2..4]. An entry holds
+// the phase e^{i phi} as i^q e^{i phi'} with |phi'| <= pi/4: (x, y) is
+// rotated by phi' with three shears, x += t y, y += s x, x += t y
+// (t = -tan(phi'/2), s = sin phi'), then multiplied by i^q: swapped when q is
+// odd and the sign words xored into the high halves of x and y.
+struct alignas(32) PhaseEntry {
+  double t;
+  double s;
+  uint32_t swap_xy;
+  uint32_t sign_x;  // 0 or 0x80000000
+  uint32_t sign_y;
+  uint32_t pad;
+};
+static_assert(sizeof(PhaseEntry) == 32, "PhaseEntry layout");
+constexpr int kMaxPhaseGlobals = 3;
 
 // Register phases of a fused pass run by the TMA window kernel: each thread
 // keeps 2^rb amplitudes of the tile in registers, the ones that differ in rb
@@ -125,6 +146,19 @@ int64_t assign_phases(Op* ops, int64_t count, int32_t tile_bits, int32_t rb);
 // Fills op.mh / op.ml (FP32 pair: hi = nearest float, lo = nearest float of
 // the rest), op.fh / op.fl (Q.54 limbs) and op.unitary from op.m.
 void split_matrix(Op& op);
+
+// Rewrites the ops src[0 .. count) of one FP64 window pass over a tile of
+// 2^k amplitudes so that it spends fewer FP64 operations: every uncontrolled
+// unitary 2x2 becomes D1 R D2 (R a real rotation, applied as three shears;
+// D1, D2 diagonal), and the diagonal factors of the whole pass (with Z-type
+// and controlled-phase ops and the diagonals of Y-type ops) are collected
+// into as few per-amplitude phase tables as the rotations allow: a diagonal
+// factor moves later in time through exchanges (re-indexed) and through
+// rotations on other bits, and earlier into the last table when nothing in
+// between touches its bits. Appends the new ops to `dst` and the tables to
+// `tab`; returns the number of ops appended.
+int64_t rewrite_pass_fp64(const Op* src, int64_t count, int32_t k, std::vector<Op>& dst,
+                          std::vector<PhaseEntry>& tab);
 
 // Arithmetic used for complex128 storage.
 enum Arith : int32_t {
@@ -263,6 +297,8 @@ struct dmv_state_s {
   std::vector<dmv::Pass> pass_staging;   // the launches of the last plan (long phase passes split)
   std::vector<dmv::PhaseOp> phase_ops;   // compact ops of the register-phase launches
   dmv::DeviceBuffer phase_ops_dev;
+  std::vector<dmv::PhaseEntry> phase_tab;  // phase tables of the rewritten FP64 passes
+  dmv::DeviceBuffer phase_tab_dev;
   std::vector<dmv::TcStage> tc_stages;  // tensor-core passes of the last plan
   std::vector<uint16_t> tc_u;
   dmv::DeviceBuffer tc_stages_dev, tc_u_dev;
@@ -270,6 +306,9 @@ struct dmv_state_s {
   size_t pinned_bytes = 0;
   int64_t last_passes = 0, last_ops = 0, last_bytes = 0;
   int64_t last_tc_passes = 0, last_tc_blocks = 0, last_tc_swaps = 0;
+  int64_t last_phase_tab_bytes = 0;  // phase tables uploaded by the last plan
+  int64_t last_upload_bytes = 0;     // every host-to-device byte of the last plan (ops, tables, digit matrices)
+  bool fp64_rewrite = true;          // FP64 window passes as rotations and phase tables
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
   size_t amp_bytes() const { return (size_t)N * (precision == DMV_C128 ? 16 : 8); }
 };

@@ -228,6 +228,7 @@ struct TmaPassParams {
   int64_t num_tiles;
   const Op* ops;
   const PhaseOp* phase_ops;  // k_window_phases' op table (num_ops <= kMaxPhaseOps)
+  const PhaseEntry* phase_tab;  // k_window_tma: tables of the pass's OP_PHASE ops
   void* amps;        // the statevector (k_window_tma's thread stores)
   int* status;       // set to 1 when a wait gave up
 };
@@ -449,7 +450,7 @@ k_window_tma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ T
       for (int l = threadIdx.x; l < T; l += NT) tv[l] = cvt_in<P>(tg[l], e);
       __syncthreads();
     }
-    tile_apply_ops<P>(tv, T, ops, num_ops, base);
+    tile_apply_ops<P>(tv, T, ops, num_ops, base, p.phase_tab);
     if constexpr (P::kBlockScaled) tile_store_fx(tv, amps, base, T, t_off, s_slot, e);
     else tile_store<P>(tv, amps, base, T, t_off, s_slot);
     fence_proxy_async_smem();
@@ -541,7 +542,7 @@ bool tma_eligible(const Pass& ps) {
 
 template <typename P>
 int launch_window_tma(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, const PhaseOp* phase_ops_dev,
-                      cudaStream_t stream) {
+                      cudaStream_t stream, const PhaseEntry* phase_tab = nullptr) {
   if constexpr (!tma_policy<P>()) {
     (void)phase_ops_dev;
     return launch_window<P>(amps, n, ps, ops_dev, stream);
@@ -564,6 +565,7 @@ int launch_window_tma(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, 
     p.num_tiles = int64_t(1) << (n - p.k);
     p.ops = ops_dev + ps.op_begin;
     p.phase_ops = phase_ops_dev ? phase_ops_dev + ps.op_begin : nullptr;
+    p.phase_tab = phase_tab;
     p.amps = amps;
     p.status = tma_status_ptr();
     if (!p.status) return set_error(DMV_ERR_CUDA, "cannot resolve the TMA status word");
@@ -624,6 +626,8 @@ double op_multiply_adds(const Op& op, int64_t N, int arith) {
     case OP_GENERAL: per_pair = pair_arith ? 172. : fixed ? 64. : 16.; break;
     case OP_RXLIKE: per_pair = pair_arith ? 172. : fixed ? 64. : 8.; break;  // general code in those arithmetics
     case OP_SWAP: per_pair = 0.; break;
+    case OP_ROT: per_pair = 6.; break;    // FP64 only: three shears on re and on im
+    case OP_PHASE: per_pair = 6.; break;  // FP64 only: three shears per amplitude
     default: per_pair = pair_arith ? 76. : fixed ? 32. : 8.; break;
   }
   const double pairs = (double)N / 2.0;
@@ -646,9 +650,21 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   passes.clear();
   ops.assign(plan.ops.begin(), plan.ops.end());
   bool any_window = false, any_phases = false;
+  // FP64 window passes on the TMA kernel: rotations and phase tables in place of
+  // general 2x2 ops (rewrite_pass_fp64), appended to the staged ops.
+  const bool rewrite = s->precision == DMV_C128 && s->arith == ARITH_FP64 && s->fp64_rewrite;
+  s->phase_tab.clear();
   for (const Pass& ps : plan.passes) {
     const int rb = ps.kind == 1 ? window_reg_bits(s, ps) : 0;
     any_window |= ps.kind == 1;
+    if (rewrite && ps.kind == 1 && tma_eligible<PolF64>(ps)) {
+      Pass rw = ps;
+      rw.op_begin = (int64_t)ops.size();
+      std::vector<Op> src(plan.ops.begin() + ps.op_begin, plan.ops.begin() + ps.op_begin + ps.op_count);
+      rw.op_count = rewrite_pass_fp64(src.data(), ps.op_count, ps.low_bits + ps.num_high, ops, s->phase_tab);
+      passes.push_back(rw);
+      continue;
+    }
     if (rb <= 0) {
       passes.push_back(ps);
       continue;
@@ -681,6 +697,13 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     phase_ops_dev = static_cast<const PhaseOp*>(s->phase_ops_dev.ptr);
   }
   const Op* ops_dev = static_cast<const Op*>(s->ops_dev.ptr);
+  const PhaseEntry* phase_tab_dev = nullptr;
+  if (!s->phase_tab.empty()) {
+    DMV_TRY(s->phase_tab_dev.reserve(s->phase_tab.size() * sizeof(PhaseEntry)));
+    DMV_CUDA_TRY(cudaMemcpyAsync(s->phase_tab_dev.ptr, s->phase_tab.data(), s->phase_tab.size() * sizeof(PhaseEntry),
+                                 cudaMemcpyHostToDevice, s->stream));
+    phase_tab_dev = static_cast<const PhaseEntry*>(s->phase_tab_dev.ptr);
+  }
   // Tensor-core arithmetic: the stages and block digit matrices of every
   // window pass it takes, uploaded once for the whole plan.
   const bool tc = s->precision == DMV_C128 && s->arith == ARITH_TC;
@@ -736,9 +759,9 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     if (arith == ARITH_TC) arith = ARITH_INT64;
     if (arith == ARITH_INT64)
       for (int64_t o = 0; o < ps.op_count; ++o)
-        if (!plan.ops[(size_t)(ps.op_begin + o)].unitary) arith = ARITH_FP64;
+        if (!ops[(size_t)(ps.op_begin + o)].unitary) arith = ARITH_FP64;
     if (ps.kind == 0) {
-      const Op& op = plan.ops[(size_t)ps.op_begin];
+      const Op& op = ops[(size_t)ps.op_begin];
       const int64_t b = op.ctrl_kind != CTRL_NONE ? S : 2 * S;
       const int64_t tok = prof_begin(DMV_KERNEL_SINGLE, s->stream, (double)b, op_multiply_adds(op, s->N, arith));
       if (s->precision == DMV_C64) launch_single<PolF32>(s->amps, s->n, op, s->stream);
@@ -750,14 +773,14 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     } else {
       double fmas = 0.;
       for (int64_t o = 0; o < ps.op_count; ++o)
-        fmas += op_multiply_adds(plan.ops[(size_t)(ps.op_begin + o)], s->N, arith);
+        fmas += op_multiply_adds(ops[(size_t)(ps.op_begin + o)], s->N, arith);
       const int64_t tok = prof_begin(DMV_KERNEL_WINDOW, s->stream, (double)(2 * S), fmas);
       void* a = s->amps;
       cudaStream_t st = s->stream;
       if (s->precision == DMV_C64) DMV_TRY(launch_window_tma<PolF32>(a, s->n, ps, ops_dev, phase_ops_dev, st));
       else if (arith == ARITH_FP32X2) DMV_TRY(launch_window_tma<PolDF>(a, s->n, ps, ops_dev, phase_ops_dev, st));
       else if (arith == ARITH_INT64) DMV_TRY(launch_window_tma<PolFX>(a, s->n, ps, ops_dev, phase_ops_dev, st));
-      else DMV_TRY(launch_window_tma<PolF64>(a, s->n, ps, ops_dev, phase_ops_dev, st));
+      else DMV_TRY(launch_window_tma<PolF64>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab_dev));
       prof_end(tok, s->stream);
       bytes += 2 * S;
     }
@@ -773,6 +796,10 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     }
   s->last_passes = (int64_t)passes.size();
   s->last_ops = (int64_t)plan.ops.size();
+  s->last_phase_tab_bytes = (int64_t)(s->phase_tab.size() * sizeof(PhaseEntry));
+  s->last_upload_bytes = s->last_phase_tab_bytes + (any_window ? (int64_t)(ops.size() * sizeof(Op)) : 0) +
+                         (any_phases ? (int64_t)(s->phase_ops.size() * sizeof(PhaseOp)) : 0) +
+                         (tc ? (int64_t)(s->tc_stages.size() * sizeof(TcStage) + s->tc_u.size() * 2) : 0);
   s->last_bytes = bytes;
   return DMV_OK;
 }

@@ -8,6 +8,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "complex_ops.cuh"
 #include "df.cuh"
 #include "fx.cuh"
@@ -302,14 +304,92 @@ __device__ __forceinline__ void tile_op(typename P::T* tile, int T, const Op& op
   }
 }
 
+// OP_ROT (FP64 window passes): the real rotation [[c, -s], [s, c]] of every
+// pair along op.target, on the real parts and on the imaginary parts, as
+// three shears: x0 += T x1, x1 += S x0, x0 += T x1 with T = -tan(t/2) =
+// op.m[0], S = sin t = op.m[1] (3 multiply-adds per amplitude). Two pairs per
+// iteration, as in tile_op.
+__device__ __forceinline__ void rot_pair(double Tq, double Sq, double2& a0, double2& a1) {
+  double x0 = a0.x, x1 = a1.x, y0 = a0.y, y1 = a1.y;
+  x0 = fma(Tq, x1, x0);
+  y0 = fma(Tq, y1, y0);
+  x1 = fma(Sq, x0, x1);
+  y1 = fma(Sq, y0, y1);
+  x0 = fma(Tq, x1, x0);
+  y0 = fma(Tq, y1, y0);
+  a0 = make_double2(x0, y0);
+  a1 = make_double2(x1, y1);
+}
+
+__device__ __forceinline__ void tile_rot(double2* tile, int T, const Op& op) {
+  const double Tq = op.m[0], Sq = op.m[1];
+  const int t = op.target;
+  const int half = T >> 1;
+  const int bd = blockDim.x;
+  for (int q = threadIdx.x; q < half; q += 2 * bd) {
+    const int q2 = q + bd;
+    const uint32_t l0 = insert_zero32((uint32_t)q, t), l1 = l0 | (1u << t);
+    double2 a0 = tile[l0], a1 = tile[l1];
+    if (q2 < half) {
+      const uint32_t m0 = insert_zero32((uint32_t)q2, t), m1 = m0 | (1u << t);
+      double2 b0 = tile[m0], b1 = tile[m1];
+      rot_pair(Tq, Sq, a0, a1);
+      rot_pair(Tq, Sq, b0, b1);
+      tile[m0] = b0;
+      tile[m1] = b1;
+    } else {
+      rot_pair(Tq, Sq, a0, a1);
+    }
+    tile[l0] = a0;
+    tile[l1] = a1;
+  }
+}
+
+// OP_PHASE (FP64 window passes): amplitude l times the phase of table entry
+// op.fh[0] + (gsel << k) + l (PhaseEntry: three shears, then a swap and sign
+// flips for the factor i^q on the integer pipe). gsel holds the tile's bits at
+// the op.fh[1] global qubits op.fh[2..].
+__device__ __forceinline__ void tile_phase(double2* tile, int T, const Op& op, const PhaseEntry* tab, int64_t base) {
+  const int k = 31 - __clz(T);
+  int gsel = 0;
+  for (int j = 0; j < op.fh[1]; ++j) gsel |= (int)((base >> op.fh[2 + j]) & 1) << j;
+  const PhaseEntry* e = tab + op.fh[0] + ((int64_t)gsel << k);
+#pragma unroll 4
+  for (int l = threadIdx.x; l < T; l += blockDim.x) {
+    const double2 ts = __ldg(reinterpret_cast<const double2*>(e + l));
+    const uint4 fl = __ldg(reinterpret_cast<const uint4*>(e + l) + 1);
+    const double2 v = tile[l];
+    const double x1 = fma(ts.x, v.y, v.x);
+    const double y1 = fma(ts.y, x1, v.y);
+    const double x2 = fma(ts.x, y1, x1);
+    const double ox = fl.x ? y1 : x2;
+    const double oy = fl.x ? x2 : y1;
+    tile[l] = make_double2(__hiloint2double(__double2hiint(ox) ^ (int)fl.y, __double2loint(ox)),
+                           __hiloint2double(__double2hiint(oy) ^ (int)fl.z, __double2loint(oy)));
+  }
+}
+
 // Every op of a pass on one tile; `base` holds the tile's global index bits
 // (controls outside the tile are read from it). Ends with a barrier after
-// each applied op.
+// each applied op. `tab` holds the phase tables of OP_PHASE ops (FP64 only).
 template <typename P>
-__device__ __forceinline__ void tile_apply_ops(typename P::T* tile, int T, const Op* ops, int num_ops, int64_t base) {
+__device__ __forceinline__ void tile_apply_ops(typename P::T* tile, int T, const Op* ops, int num_ops, int64_t base,
+                                               const PhaseEntry* tab = nullptr) {
   for (int o = 0; o < num_ops; ++o) {
     const Op& op = ops[o];
     if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1)) continue;  // uniform per tile
+    if constexpr (std::is_same<typename P::T, double2>::value && std::is_same<typename P::G, double2>::value) {
+      if (op.cls == OP_ROT) {
+        tile_rot(tile, T, op);
+        __syncthreads();
+        continue;
+      }
+      if (op.cls == OP_PHASE) {
+        tile_phase(tile, T, op, tab, base);
+        __syncthreads();
+        continue;
+      }
+    }
     switch (op.cls) {
       case OP_SWAP: tile_op<P, OP_SWAP>(tile, T, op); break;
       case OP_DIAG: tile_op<P, OP_DIAG>(tile, T, op); break;

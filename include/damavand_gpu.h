@@ -53,7 +53,13 @@ enum { DMV_C128 = 0, DMV_C64 = 1 };
 
 /* Arithmetic of complex128 gate application (complex64 always computes in FP32).
  * The amplitudes stay IEEE complex128 in device memory in every mode.
- * DMV_ARITH_FP64: IEEE FP64 multiply-adds (default).
+ * DMV_ARITH_FP64: IEEE FP64 arithmetic (default). Fused window passes on the
+ *   TMA kernel write each uncontrolled unitary 2x2 as diagonal x real rotation
+ *   x diagonal, apply the rotation as three shears (3 FP64 multiply-adds per
+ *   amplitude instead of 8) and collect the diagonals of a pass into a few
+ *   per-amplitude phase tables, each applied with three more shears.
+ * DMV_ARITH_FP64_DIRECT: IEEE FP64 with every fused 2x2 applied as a full
+ *   complex multiply-add (8 per amplitude for a general matrix).
  * DMV_ARITH_FP32X2: the FP64 amplitudes are split into FP32 pairs (about 48
  *   significant bits) inside each kernel and combined with error-free
  *   transformations, then stored back as FP64; GB300 runs FP32 ~71x faster
@@ -70,7 +76,7 @@ enum { DMV_C128 = 0, DMV_C64 = 1 };
  *   accumulators in tensor memory, every sum exact), rounded once per
  *   output. Passes it does not take run as DMV_ARITH_INT64. Single states
  *   only (batches accept FP64, FP32X2 and INT64). */
-enum { DMV_ARITH_FP64 = 0, DMV_ARITH_FP32X2 = 1, DMV_ARITH_INT64 = 2, DMV_ARITH_TC = 3 };
+enum { DMV_ARITH_FP64 = 0, DMV_ARITH_FP32X2 = 1, DMV_ARITH_INT64 = 2, DMV_ARITH_TC = 3, DMV_ARITH_FP64_DIRECT = 4 };
 
 /* Gate kinds (numbering shared with the oracle). DMV_GATE_MATRIX takes an
  * explicit 2x2 matrix; every kind may carry a control qubit. */
@@ -177,6 +183,11 @@ int dmv_last_plan_stats(int64_t* num_passes, int64_t* num_fused_ops, int64_t* by
  * DMV_ARITH_TC: window passes that ran on the tensor cores, their dense
  * blocks and their exchange stages (zeros for other arithmetics). */
 int dmv_last_tc_stats(dmv_state_t s, int64_t* tc_passes, int64_t* blocks, int64_t* exchanges);
+/* Bytes the last gate application on `s` copied from the host to the device
+ * (the plan's op list, phase tables, tensor-core stages and digit matrices),
+ * and of those the phase tables of the FP64 rotation passes. No reference
+ * counterpart. */
+int dmv_last_upload_bytes(dmv_state_t s, int64_t* total, int64_t* phase_tables);
 /* Plans a gate list without touching a GPU (host only): the number of HBM
  * passes, of window passes, of ops after merging, and the largest number of
  * local qubits of a window. tile_bits 0 picks the default for the precision. */
@@ -285,6 +296,15 @@ int dmv_debug_tc_convert(int32_t mode);
  * leaves the state undefined and the next dmv_state_synchronize returns
  * DMV_ERR_TIMEOUT. No reference counterpart. */
 int dmv_debug_tma_wait_limit(int64_t polls);
+/* Test hook (host only, no GPU): plans `gates` for num_qubits (12..34) with
+ * 2^12-amplitude windows, rewrites every window pass the FP64 TMA kernel takes
+ * into rotations and phase tables (DMV_ARITH_FP64), applies the original and
+ * the rewritten ops to two random tiles each in host FP64, and returns the
+ * largest normwise difference. counts (may be NULL) receives 4 values: passes
+ * checked, non-exchange ops before, rotations and phase tables after. No
+ * reference counterpart. */
+int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num_gates, int32_t num_qubits, uint64_t seed,
+                                 double* max_err, int64_t* counts);
 
 /* ------------------------------------------------------------------------ */
 /* Circuit front-end (the reference's pyo3 Circuit, src/qubit_backend/circuit.rs:78-770) */

@@ -202,40 +202,78 @@ void orc_sample(const double* probs, int64_t num_probs, const double* uniforms,
   free(cdf);
 }
 
-/* Exact Pauli-Z expectation; sign convention of circuit.rs:503-508 (+1 for bit 0). */
-void orc_expect_z(const double* probs, int32_t n, double* out) {
-  int64_t N = (int64_t)1 << n;
-  for (int32_t q = 0; q < n; ++q) {
-    double acc = 0.;
-#pragma omp parallel for schedule(static) reduction(+ : acc)
-    for (int64_t i = 0; i < N; ++i) acc += ((i >> q) & 1) ? -probs[i] : probs[i];
-    out[q] = acc;
-  }
+/* Compensated accumulation (Neumaier's variant of Kahan summation). */
+static inline void acc_add(double* s, double* c, double x) {
+  double t = *s + x;
+  if (fabs(*s) >= fabs(x)) *c += (*s - t) + x;
+  else *c += (x - t) + *s;
+  *s = t;
 }
 
-/* The same <Z_q> straight from the amplitudes (p_i = norm_sqr, circuit.rs:579-581)
- * in one pass, for states whose probability vector would not fit beside them. */
+/* Per-bit masses of p_0 .. p_{N-1}: out[q] = sum of p_i with bit q of i set,
+ * total = sum of all. Blocks of 1024 consecutive indices are summed plainly
+ * (bits 0-9 inside the block, the block's total for the bits above) and the
+ * block sums accumulate with compensation, so the error stays near one
+ * rounding of each block sum even at 2^31 terms (a plain running sum of 2^30
+ * similar terms drifts by ~1e-10). `get(i)` is p_i. */
+#define ORC_BLOCK_BITS 10
+#define ORC_BIT_MASSES(N, n, GET, out, total_out)                                  \
+  do {                                                                             \
+    double tot_s = 0., tot_c = 0.;                                                 \
+    double set_s[64], set_c[64];                                                   \
+    for (int32_t q = 0; q < (n); ++q) set_s[q] = set_c[q] = 0.;                     \
+    int64_t bsz = (int64_t)1 << ((n) < ORC_BLOCK_BITS ? (n) : ORC_BLOCK_BITS);      \
+    int64_t nblk = (N) / bsz;                                                      \
+    _Pragma("omp parallel")                                                        \
+    {                                                                              \
+      double ts = 0., tc = 0., ss[64], sc[64];                                     \
+      for (int32_t q = 0; q < (n); ++q) ss[q] = sc[q] = 0.;                         \
+      _Pragma("omp for schedule(static) nowait")                                   \
+      for (int64_t b = 0; b < nblk; ++b) {                                         \
+        double bt = 0., bb[ORC_BLOCK_BITS];                                        \
+        for (int j = 0; j < ORC_BLOCK_BITS; ++j) bb[j] = 0.;                       \
+        for (int64_t e = 0; e < bsz; ++e) {                                        \
+          int64_t i = b * bsz + e;                                                 \
+          double p = GET(i);                                                       \
+          bt += p;                                                                 \
+          for (int j = 0; j < ORC_BLOCK_BITS; ++j)                                 \
+            if ((e >> j) & 1) bb[j] += p;                                          \
+        }                                                                          \
+        acc_add(&ts, &tc, bt);                                                     \
+        for (int32_t q = 0; q < (n); ++q) {                                         \
+          if (q < ORC_BLOCK_BITS) { if ((int64_t)1 << q < bsz) acc_add(&ss[q], &sc[q], bb[q]); } \
+          else if ((b >> (q - ORC_BLOCK_BITS)) & 1) acc_add(&ss[q], &sc[q], bt);   \
+        }                                                                          \
+      }                                                                            \
+      _Pragma("omp critical")                                                      \
+      {                                                                            \
+        acc_add(&tot_s, &tot_c, ts + tc);                                          \
+        for (int32_t q = 0; q < (n); ++q) acc_add(&set_s[q], &set_c[q], ss[q] + sc[q]); \
+      }                                                                            \
+    }                                                                              \
+    for (int32_t q = 0; q < (n); ++q) (out)[q] = set_s[q] + set_c[q];               \
+    *(total_out) = tot_s + tot_c;                                                  \
+  } while (0)
+
+/* Exact Pauli-Z expectation; sign convention of circuit.rs:503-508 (+1 for bit 0):
+ * <Z_q> = total - 2 * (mass with bit q set). */
+void orc_expect_z(const double* probs, int32_t n, double* out) {
+  int64_t N = (int64_t)1 << n;
+  double total = 0.;
+#define ORC_GET_P(i) (probs[(i)])
+  ORC_BIT_MASSES(N, n, ORC_GET_P, out, &total);
+#undef ORC_GET_P
+  for (int32_t q = 0; q < n; ++q) out[q] = total - 2. * out[q];
+}
+
+/* The same <Z_q> straight from the amplitudes (p_i = norm_sqr, circuit.rs:579-581),
+ * for states whose probability vector would not fit beside them. */
 void orc_expect_z_from_state(const double* state, int32_t n, double* out) {
   int64_t N = (int64_t)1 << n;
   double total = 0.;
-  for (int32_t q = 0; q < n; ++q) out[q] = 0.;
-#pragma omp parallel
-  {
-    double set[64] = {0.};
-    double tot = 0.;
-#pragma omp for schedule(static) nowait
-    for (int64_t i = 0; i < N; ++i) {
-      double p = state[2 * i] * state[2 * i] + state[2 * i + 1] * state[2 * i + 1];
-      tot += p;
-      for (int32_t q = 0; q < n; ++q)
-        if ((i >> q) & 1) set[q] += p;
-    }
-#pragma omp critical
-    {
-      total += tot;
-      for (int32_t q = 0; q < n; ++q) out[q] += set[q];
-    }
-  }
+#define ORC_GET_A(i) (state[2 * (i)] * state[2 * (i)] + state[2 * (i) + 1] * state[2 * (i) + 1])
+  ORC_BIT_MASSES(N, n, ORC_GET_A, out, &total);
+#undef ORC_GET_A
   for (int32_t q = 0; q < n; ++q) out[q] = total - 2. * out[q];
 }
 
