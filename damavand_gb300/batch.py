@@ -16,7 +16,8 @@ from . import _lib
 from ._lib import Gate, check, dptr, lib
 
 _PREC = {"complex128": _lib.C128, "complex64": _lib.C64}
-_ARITH = {"fp64": _lib.ARITH_FP64, "fp32x2": _lib.ARITH_FP32X2, "int64": _lib.ARITH_INT64}
+_ARITH = {"fp64": _lib.ARITH_FP64, "fp64-direct": _lib.ARITH_FP64_DIRECT, "fp32x2": _lib.ARITH_FP32X2,
+          "int64": _lib.ARITH_INT64}
 
 
 class Batch:

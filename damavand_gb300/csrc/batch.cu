@@ -52,7 +52,8 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 template <typename P>
 __global__ void __launch_bounds__(kBatchThreads, 2)
 k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes, const BatchItem* __restrict__ items,
-        int64_t num_items, const Op* __restrict__ ops, unsigned long long* counters, long long spin_limit) {
+        int64_t num_items, const Op* __restrict__ ops, const PhaseEntry* __restrict__ phase_tab,
+        unsigned long long* counters, long long spin_limit) {
   using V = typename P::T;
   using G = typename P::G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -98,12 +99,12 @@ k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes,
       if constexpr (P::kBlockScaled) {
         const int e = tile_load_fx<true>(tile, a, base, T, t_off, s_slot, s_red);
         __syncthreads();
-        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
+        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base, phase_tab);
         tile_store_fx(tile, a, base, T, t_off, s_slot, e);
       } else {
         tile_load<P, true>(tile, a, base, T, t_off, s_slot);
         __syncthreads();
-        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
+        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base, phase_tab);
         tile_store<P>(tile, a, base, T, t_off, s_slot);
       }
       __syncthreads();
@@ -134,13 +135,14 @@ struct dmv_batch_s {
   int32_t count = 0;
   int32_t precision = DMV_C128;
   int32_t arith = ARITH_FP64;
+  bool fp64_rewrite = true;  // FP64 passes as rotations and phase tables (rewrite_pass_fp64)
   std::vector<int32_t> n;
   std::vector<std::vector<Gate>> gates;
   std::vector<int64_t> offsets;  // amplitudes
   int64_t total_amps = 0;
   void* arena = nullptr;
   cudaStream_t stream = nullptr;
-  DeviceBuffer passes_dev, items_dev, ops_dev, counters_dev, offsets_dev, reduce_dev;
+  DeviceBuffer passes_dev, items_dev, ops_dev, counters_dev, offsets_dev, reduce_dev, phase_tab_dev;
   std::vector<int64_t> red_mass, red_partial, red_sums;  // per-circuit offsets (doubles) into reduce_dev
   int64_t num_items = 0, num_passes = 0, num_ops = 0;
   int32_t max_k = 0;
@@ -172,6 +174,8 @@ void destroy_graph(dmv_batch_s* b) {
 int batch_plan(dmv_batch_s* b) {
   std::vector<BatchPass> passes;
   std::vector<Op> ops;
+  std::vector<PhaseEntry> tab;
+  const bool rewrite = b->precision == DMV_C128 && b->arith == ARITH_FP64 && b->fp64_rewrite;
   std::vector<std::vector<int32_t>> pass_ids((size_t)b->count);
   std::vector<std::vector<int64_t>> pass_tiles((size_t)b->count);
   b->max_k = 0;
@@ -190,7 +194,11 @@ int batch_plan(dmv_batch_s* b) {
       for (int i = 0; i < p.num_high; ++i) bp.high[i] = p.high[i];
       bp.amp_offset = b->offsets[(size_t)c];
       bp.op_begin = (int64_t)ops.size();
-      for (int64_t o = 0; o < p.op_count; ++o) ops.push_back(plan.ops[(size_t)(p.op_begin + o)]);
+      if (rewrite) {
+        bp.num_ops = (int32_t)rewrite_pass_fp64(plan.ops.data() + p.op_begin, p.op_count, bp.k, ops, tab);
+      } else {
+        for (int64_t o = 0; o < p.op_count; ++o) ops.push_back(plan.ops[(size_t)(p.op_begin + o)]);
+      }
       b->max_k = std::max(b->max_k, bp.k);
       pass_ids[(size_t)c].push_back((int32_t)passes.size());
       pass_tiles[(size_t)c].push_back(int64_t(1) << (b->n[(size_t)c] - bp.k));
@@ -245,6 +253,9 @@ int batch_plan(dmv_batch_s* b) {
     DMV_CUDA_TRY(cudaMemcpy(b->items_dev.ptr, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
   if (!ops.empty())
     DMV_CUDA_TRY(cudaMemcpy(b->ops_dev.ptr, ops.data(), ops.size() * sizeof(Op), cudaMemcpyHostToDevice));
+  DMV_TRY(b->phase_tab_dev.reserve(std::max<size_t>(1, tab.size()) * sizeof(PhaseEntry)));
+  if (!tab.empty())
+    DMV_CUDA_TRY(cudaMemcpy(b->phase_tab_dev.ptr, tab.data(), tab.size() * sizeof(PhaseEntry), cudaMemcpyHostToDevice));
   return DMV_OK;
 }
 
@@ -274,6 +285,7 @@ int batch_launch_kernel(dmv_batch_s* b) {
                                   static_cast<const BatchPass*>(b->passes_dev.ptr),
                                   static_cast<const BatchItem*>(b->items_dev.ptr), b->num_items,
                                   static_cast<const Op*>(b->ops_dev.ptr),
+                                  static_cast<const PhaseEntry*>(b->phase_tab_dev.ptr),
                                   static_cast<unsigned long long*>(b->counters_dev.ptr), b->spin_limit));
   count_launch();
   return DMV_OK;
@@ -361,7 +373,8 @@ extern "C" int dmv_batch_create(int32_t num_circuits, const int32_t* num_qubits,
   *out = nullptr;
   if (num_circuits < 1 || !num_qubits || !gate_offsets) return set_error(DMV_ERR_INVALID, "empty batch");
   if (precision != DMV_C128 && precision != DMV_C64) return set_error(DMV_ERR_INVALID, "unknown precision");
-  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2 && arithmetic != DMV_ARITH_INT64)
+  if (arithmetic != DMV_ARITH_FP64 && arithmetic != DMV_ARITH_FP32X2 && arithmetic != DMV_ARITH_INT64 &&
+      arithmetic != DMV_ARITH_FP64_DIRECT)
     return set_error(DMV_ERR_INVALID, "unknown arithmetic");
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
@@ -371,7 +384,8 @@ extern "C" int dmv_batch_create(int32_t num_circuits, const int32_t* num_qubits,
   dmv_batch_s* b = new dmv_batch_s();
   b->count = num_circuits;
   b->precision = precision;
-  b->arith = arithmetic;
+  b->arith = arithmetic == DMV_ARITH_FP64_DIRECT ? (int32_t)ARITH_FP64 : arithmetic;
+  b->fp64_rewrite = arithmetic == DMV_ARITH_FP64;
   int64_t off = 0;
   for (int32_t c = 0; c < num_circuits; ++c) {
     const int32_t n = num_qubits[c];

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "complex_ops.cuh"
+#include "df.cuh"
 #include "internal.h"
 #include "policies.cuh"
 
@@ -148,6 +149,153 @@ k_chunk_mass(const void* src, int n, int chunk_bits, int64_t num_chunks,
     for (int j = 0; j < n - chunk_bits; ++j) out[chunk_bits + j] = hi_acc[j];
   }
 }
+
+// ---------------------------------------------------------------------------
+// The same per-chunk and per-bit masses in FP32 pairs (k_chunk_mass_f2).
+//
+// On GB300 the FP64 reduction above spends 4 FP64 operations per amplitude
+// and runs at about a third of HBM speed. Here every probability is formed
+// and summed as an unevaluated pair of floats hi + lo: the components of a
+// complex128 amplitude are split into FP32 pairs with integer operations
+// (split_f64), x^2 is hi^2 exactly by FMA (TwoProd) plus the cross terms,
+// and sums use Knuth's TwoSum with the error kept in lo and the pair
+// renormalised (Fast2Sum) after each addition. Each accumulator holds about
+// 46 significant bits: the probabilities' relative error is at most ~2^-45,
+// and an accumulator of k additions drifts by at most ~k 2^-47 of its value
+// (k <= 2^17 per accumulator at 34 qubits). Amplitudes below 2^-126 count as
+// zero (FP32 range; their probabilities are below 2^-252). FP64 runs once per
+// accumulator at the end.
+// ---------------------------------------------------------------------------
+struct F2 {
+  float h, l;
+};
+
+__device__ __forceinline__ void f2_add(F2& a, float bh, float bl) {
+  const float t = __fadd_rn(a.h, bh);  // TwoSum(a.h, bh) = t + e exactly
+  const float z = __fsub_rn(t, a.h);
+  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(t, z)), __fsub_rn(bh, z));
+  const float c = __fadd_rn(a.l, __fadd_rn(e, bl));
+  a.h = __fadd_rn(t, c);  // Fast2Sum(t, c): |t| >= |c|
+  a.l = __fsub_rn(c, __fsub_rn(a.h, t));
+}
+
+// |x|^2 + |y|^2 of one amplitude as an FP32 pair.
+template <int SRC>
+__device__ __forceinline__ F2 f2_prob(const void* src, int64_t i) {
+  float xh, xl, yh, yl;
+  if constexpr (SRC == 0) {
+    const double2 a = static_cast<const double2*>(src)[i];
+    split_f64(a.x, xh, xl);
+    split_f64(a.y, yh, yl);
+  } else {
+    const float2 a = static_cast<const float2*>(src)[i];
+    xh = a.x; yh = a.y;
+    xl = 0.f; yl = 0.f;
+  }
+  const float px = __fmul_rn(xh, xh), py = __fmul_rn(yh, yh);
+  float ex = __fmaf_rn(xh, xh, -px);  // exact error of hi^2
+  float ey = __fmaf_rn(yh, yh, -py);
+  ex = __fmaf_rn(__fadd_rn(xh, xh), xl, ex);  // + 2 hi lo
+  ey = __fmaf_rn(__fadd_rn(yh, yh), yl, ey);
+  ex = __fmaf_rn(xl, xl, ex);  // + lo^2
+  ey = __fmaf_rn(yl, yl, ey);
+  F2 r{px, __fadd_rn(ex, ey)};
+  f2_add(r, py, 0.f);
+  return r;
+}
+
+__device__ __forceinline__ double f2_val(const F2& a) { return (double)a.h + (double)a.l; }
+
+__device__ __forceinline__ F2 f2_warp_sum(F2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, v.h, o);
+    const float l = __shfl_xor_sync(0xffffffffu, v.l, o);
+    f2_add(v, h, l);
+  }
+  return v;
+}
+
+constexpr int kF2Rows = 16;  // chunk of kRedThreads x 16 = 4096 amplitudes
+constexpr int kF2ChunkBits = 12;
+
+// As k_chunk_mass (same outputs: chunk_mass[ch], and per CTA the n + 1 sums
+// `partial`), in FP32 pairs, for complex128 (SRC 0) and complex64 (SRC 1)
+// amplitudes, with 4096-amplitude chunks (chunk_bits = min(n, 12)).
+template <int SRC>
+__global__ void __launch_bounds__(kRedThreads)
+k_chunk_mass_f2(const void* src, int n, int chunk_bits, int64_t num_chunks, double* __restrict__ chunk_mass,
+                double* __restrict__ partial) {
+  __shared__ F2 red[kRedThreads / 32];
+  __shared__ double tsum[kRedThreads];
+  __shared__ double rsum[4][kRedThreads];
+  __shared__ double hi_acc[34];  // only thread 0 updates it
+  const int C = 1 << chunk_bits;
+  F2 v[kF2Rows];
+#pragma unroll
+  for (int r = 0; r < kF2Rows; ++r) v[r] = F2{0.f, 0.f};
+  if (threadIdx.x < 34) hi_acc[threadIdx.x] = 0.;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t ch = blockIdx.x; ch < num_chunks; ch += gridDim.x) {
+    const int64_t base = ch << chunk_bits;
+    F2 mine{0.f, 0.f};
+#pragma unroll
+    for (int r = 0; r < kF2Rows; ++r) {
+      const int e = threadIdx.x + kRedThreads * r;
+      if (e < C) {
+        const F2 p = f2_prob<SRC>(src, base + e);
+        f2_add(v[r], p.h, p.l);
+        f2_add(mine, p.h, p.l);
+      }
+    }
+    mine = f2_warp_sum(mine);
+    __syncthreads();
+    if (lane == 0) red[warp] = mine;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      F2 tot{0.f, 0.f};
+      for (int w = 0; w < kRedThreads / 32; ++w) f2_add(tot, red[w].h, red[w].l);
+      const double t = f2_val(tot);
+      chunk_mass[ch] = t;
+      for (int j = 0; j < n - chunk_bits; ++j)
+        if ((ch >> j) & 1) hi_acc[j] += t;
+    }
+  }
+  double T = 0.;
+  double R[4] = {0., 0., 0., 0.};
+#pragma unroll
+  for (int r = 0; r < kF2Rows; ++r) {
+    const double x = f2_val(v[r]);
+    T += x;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if ((r >> j) & 1) R[j] += x;
+  }
+  tsum[threadIdx.x] = T;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) rsum[j][threadIdx.x] = R[j];
+  __syncthreads();
+  double* out = partial + (int64_t)blockIdx.x * (n + 1);
+  const int q = threadIdx.x;
+  if (q < chunk_bits) {
+    double acc = 0.;
+    if (q < 8) {
+      for (int t = 0; t < kRedThreads; ++t)
+        if ((t >> q) & 1) acc += tsum[t];
+    } else {
+      for (int t = 0; t < kRedThreads; ++t) acc += rsum[q - 8][t];
+    }
+    out[q] = acc;
+  } else if (q == kRedThreads - 1) {
+    double acc = 0.;
+    for (int t = 0; t < kRedThreads; ++t) acc += tsum[t];
+    out[n] = acc;
+  }
+  if (threadIdx.x == 0)
+    for (int j = 0; j < n - chunk_bits; ++j) out[chunk_bits + j] = hi_acc[j];
+}
+static_assert((1 << kF2ChunkBits) == kRedThreads * kF2Rows, "a chunk is one amplitude per thread and row");
+static_assert(kF2ChunkBits < kRedThreads - 1, "the total's thread is not a per-bit thread");
 
 // Sum the per-CTA partials in CTA order.
 __global__ void k_reduce_partials(const double* __restrict__ partial, int width, int rows,
@@ -493,6 +641,19 @@ k_adjoint_step(typename P::G* __restrict__ psi, typename P::G* __restrict__ lam,
 }
 
 int chunk_bits_for(int n) { return std::min(kMaxChunkBits, n); }
+// Chunks of the Pauli-Z mass pass (k_chunk_mass_f2): 4096 amplitudes.
+int mass_chunk_bits_for(int n) { return std::min(kF2ChunkBits, n); }
+
+// The per-chunk / per-bit mass pass: FP32 pairs for amplitudes (src_kind 0
+// complex128, 1 complex64), FP64 for a probability vector (src_kind 2).
+void launch_mass_kernel(const void* src, int src_kind, int n, int cb, int64_t num_chunks, int grid, double* mass,
+                        double* partial, cudaStream_t stream) {
+  switch (src_kind) {
+    case 0: k_chunk_mass_f2<0><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
+    case 1: k_chunk_mass_f2<1><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
+    default: k_chunk_mass<2><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
+  }
+}
 
 int grid_for_chunks(int64_t num_chunks) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(num_chunks, (int64_t)sm_count() * 8));
@@ -503,7 +664,7 @@ int grid_for_chunks(int64_t num_chunks) {
 int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& chunk_dev,
                     DeviceBuffer& reduce_dev, cudaStream_t stream, double** sums_dev_out,
                     int64_t* num_chunks_out, int* chunk_bits_out) {
-  const int cb = chunk_bits_for(n);
+  const int cb = src_kind == 2 ? chunk_bits_for(n) : mass_chunk_bits_for(n);
   const int64_t num_chunks = int64_t(1) << (n - cb);
   const int grid = grid_for_chunks(num_chunks);
   DMV_TRY(chunk_dev.reserve((size_t)num_chunks * sizeof(double)));
@@ -512,11 +673,7 @@ int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& chunk_de
   double* partial = static_cast<double*>(reduce_dev.ptr);
   double* sums = partial + partial_elems;
   double* mass = static_cast<double*>(chunk_dev.ptr);
-  switch (src_kind) {
-    case 0: k_chunk_mass<0><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
-    case 1: k_chunk_mass<1><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
-    default: k_chunk_mass<2><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
-  }
+  launch_mass_kernel(src, src_kind, n, cb, num_chunks, grid, mass, partial, stream);
   k_reduce_partials<<<1, 64, 0, stream>>>(partial, n + 1, grid, sums);
   count_launch(2);
   DMV_CUDA_TRY(cudaGetLastError());
@@ -599,7 +756,7 @@ int run_sampler(const void* src, int src_kind, int n, DeviceBuffer& prefix, Devi
 
 ChunkMassShape chunk_mass_shape(int n) {
   ChunkMassShape sh;
-  sh.chunk_bits = chunk_bits_for(n);
+  sh.chunk_bits = mass_chunk_bits_for(n);
   sh.num_chunks = int64_t(1) << (n - sh.chunk_bits);
   sh.grid = grid_for_chunks(sh.num_chunks);
   sh.partial_elems = (int64_t)sh.grid * (n + 1);
@@ -608,12 +765,9 @@ ChunkMassShape chunk_mass_shape(int n) {
 
 int launch_chunk_mass_into(const void* src, int src_kind, int n, double* mass, double* partial, double* sums,
                            cudaStream_t stream) {
+  if (src_kind == 2) return set_error(DMV_ERR_INVALID, "launch_chunk_mass_into takes amplitudes (kinds 0, 1)");
   const ChunkMassShape sh = chunk_mass_shape(n);
-  switch (src_kind) {
-    case 0: k_chunk_mass<0><<<sh.grid, kRedThreads, 0, stream>>>(src, n, sh.chunk_bits, sh.num_chunks, mass, partial); break;
-    case 1: k_chunk_mass<1><<<sh.grid, kRedThreads, 0, stream>>>(src, n, sh.chunk_bits, sh.num_chunks, mass, partial); break;
-    default: k_chunk_mass<2><<<sh.grid, kRedThreads, 0, stream>>>(src, n, sh.chunk_bits, sh.num_chunks, mass, partial); break;
-  }
+  launch_mass_kernel(src, src_kind, n, sh.chunk_bits, sh.num_chunks, sh.grid, mass, partial, stream);
   k_reduce_partials<<<1, 64, 0, stream>>>(partial, n + 1, sh.grid, sums);
   count_launch(2);
   DMV_CUDA_TRY(cudaGetLastError());

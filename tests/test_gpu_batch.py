@@ -12,7 +12,7 @@ def _small_batch(seed=40, count=24):
     return uneven_batch(count=count, seed=seed, min_qubits=2, max_qubits=15, min_depth=0, max_depth=8)
 
 
-@pytest.mark.parametrize("arith", ["fp64", "fp32x2"])
+@pytest.mark.parametrize("arith", ["fp64", "fp64-direct", "fp32x2", "int64"])
 def test_batch_matches_oracle_complex128(built_lib, oracle_mod, arith):
     from damavand_gb300.batch import Batch
     circuits = _small_batch()
