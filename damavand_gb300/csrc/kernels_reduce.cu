@@ -392,6 +392,36 @@ k_segment_prefix(const void* src, int seg_bits, int chunk_bits, int64_t num_chun
   }
 }
 
+// k_segment_prefix for amplitudes (SRC 0 complex128, 1 complex64) in FP32
+// pairs: the same outputs, with the probabilities formed and summed as in
+// k_chunk_mass_f2 (each segment sum and running prefix carries ~46 bits; the
+// prefixes are written as FP64). Dyadic probabilities stay exact.
+template <int SRC>
+__global__ void __launch_bounds__(kRedThreads)
+k_segment_prefix_f2(const void* src, int seg_bits, int chunk_bits, int64_t num_chunks, double* __restrict__ seg_incl,
+                    double* __restrict__ chunk_mass) {
+  const int lane = threadIdx.x & 31;
+  const int S = 1 << seg_bits, spc = 1 << (chunk_bits - seg_bits);
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += nwarps) {
+    F2 run{0.f, 0.f};
+    for (int j = 0; j < spc; ++j) {
+      const int64_t base = (c << chunk_bits) + ((int64_t)j << seg_bits);
+      F2 ls{0.f, 0.f};
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        if (lane + 32 * e < S) {
+          const F2 p = f2_prob<SRC>(src, base + lane + 32 * e);
+          f2_add(ls, p.h, p.l);
+        }
+      ls = f2_warp_sum(ls);
+      f2_add(run, ls.h, ls.l);
+      if (lane == 0) seg_incl[c * spc + j] = f2_val(run);
+    }
+    if (lane == 0) chunk_mass[c] = f2_val(run);
+  }
+}
+
 // Guide table of the chunk prefixes: guide[b] = least chunk c with
 // incl[c] >= b * (total / M) for b < M, guide[M] = the last chunk. A value
 // xsi with b * step <= xsi < (b + 1) * step has its chunk in
@@ -708,8 +738,8 @@ int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefi
   int32_t* guide = reinterpret_cast<int32_t*>(seg + nseg);
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 7) / 8, (int64_t)sm_count() * 8));
   switch (src_kind) {
-    case 0: k_segment_prefix<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
-    case 1: k_segment_prefix<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+    case 0: k_segment_prefix_f2<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+    case 1: k_segment_prefix_f2<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
     default: k_segment_prefix<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
   }
   k_scan_chunks<<<1, 1024, 0, stream>>>(mass, sp.num_chunks, incl);

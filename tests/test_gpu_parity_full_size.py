@@ -8,6 +8,9 @@
 * 31 qubits (2^31 amplitudes, past every 32-bit index): a short list that
   uses qubit 30 as target and as control, against the oracle; <Z_q> through
   dmv_expect_z and through the allocation-free entry point.
+* 32 qubits in complex64 (2^32 amplitudes, 34.4 GB): a short list through
+  the top qubits against the oracle's complex128 run, within complex64
+  accuracy.
 * 24 qubits, 1152 parameters (the adjoint configuration at full size): the
   adjoint gradient on sampled parameters against the oracle's parameter
   shift (src/qubit_backend/circuit.rs:529-546 rule) and against FP64 central
@@ -16,9 +19,10 @@
 The oracle runs with its in-place pair update (bit-identical to the
 reference's clone-per-gate sweep, pinned by the oracle tests) so that the
 host holds one statevector. Device and oracle states are compared on the
-device, 1 GB slice by slice. Host time on 16 Neoverse-V2 cores: about a
-minute for the 30-qubit oracle, about a minute for the 31-qubit one, and
-about two minutes for the sampled parameter shift at 24 qubits.
+device, 1 GB slice by slice. Host time on 16 Neoverse-V2 cores, measured:
+about 20 s each for the 30- and 31-qubit oracles and for the sampled
+parameter shift at 24 qubits; the 32-qubit oracle holds 68.7 GB of host
+memory.
 """
 import ctypes
 import math
@@ -137,3 +141,30 @@ def test_adjoint_full_size_against_oracle_param_shift_and_central_differences(bu
         assert abs((lu - ld) / (2 * h) - g[j]) < 5e-9, j
     c.set_parameters(p)
     assert abs(c.loss(w) - loss) < 1e-12
+
+
+def test_32_qubit_complex64_against_oracle(built_lib, oracle_mod):
+    """2^32 amplitudes in complex64 (34.4 GB): a short list through the top qubits
+    against the oracle's complex128 run, within complex64 accuracy; <Z_q> summed
+    from the complex64 amplitudes in FP32 pairs."""
+    import torch
+    from damavand_gb300 import Circuit
+    from damavand_gb300.workloads import CNOT, RX, RY, RZ, H, add_to_circuit
+    n = 32
+    rng = np.random.default_rng(32)
+    ang = lambda: float(rng.uniform(0.0, 2.0 * math.pi))  # noqa: E731
+    gates = [(H, q, -1, False, 0.0) for q in range(n)]
+    gates += [(RY, 31, -1, False, ang()), (CNOT, 0, 31, False, 0.0), (RX, 30, -1, False, ang()),
+              (CNOT, 31, 30, False, 0.0), (RZ, 31, -1, False, ang()), (CNOT, 31, 5, False, 0.0),
+              (RY, 0, -1, False, ang()), (CNOT, 12, 31, False, 0.0), (RX, 31, -1, False, ang())]
+    want = oracle_mod.forward(n, _og(gates), clone=False)
+    ez_want = oracle_mod.expect_z_from_state(want)
+    c = Circuit(n, "gpu", precision="complex64")
+    add_to_circuit(c, gates)
+    c.forward()
+    err = _device_normwise_err(c.state().torch(), want)
+    assert err <= 1e-5, f"complex64 normwise {err:.3e}"
+    assert np.max(np.abs(c.expectation_z() - ez_want)) <= 1e-5
+    assert abs(c.norm() - 1.0) <= 1e-5
+    del c
+    torch.cuda.empty_cache()
