@@ -491,6 +491,23 @@ def large_section(args):
                               "max_abs_diff": float(max(diffs)), "tolerance": 1e-10, "ok": bool(max(diffs) <= 1e-10)}
     del c
     torch.cuda.empty_cache()
+    if not args.no_cpu:
+        # The reference's CPU path at 31 qubits: one gate of this forward (clone + sweep of the
+        # 34.4 GB state) timed, scaled to the forward and to parameter shift (two forwards per
+        # parameter; the reference has no adjoint).
+        from oracle import oracle
+        oracle.build()
+        st31 = oracle.zero_state(n)
+        t0 = time.perf_counter()
+        oracle.forward(n, [(kk, t, cc, int(o), th) for kk, t, cc, o, th in gates[:1]], st31, clone=True)
+        t_gate = time.perf_counter() - t0
+        del st31
+        res["cpu_baseline"] = {"value": 1.0 / t_gate, "unit": "gate-applies/s", "cores": oracle.num_threads(),
+                               "kind": "port", "extrapolated": True,
+                               "forward31_s_extrapolated": t_gate * len(gates),
+                               "param_shift31_grads_per_s_extrapolated": 1.0 / (2.0 * t_gate * len(gates)),
+                               "sample": f"gate 1 of the {len(gates)}-gate 31-qubit forward on the host "
+                                         f"({t_gate:.1f} s), scaled"}
 
     m = 32
     g32 = ring_ansatz(m, 12, seed=5)
