@@ -52,7 +52,7 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 template <typename P>
 __global__ void __launch_bounds__(kBatchThreads, 2)
 k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes, const BatchItem* __restrict__ items,
-        int64_t num_items, const Op* __restrict__ ops, const PhaseEntry* __restrict__ phase_tab,
+        int64_t num_items, const Op* __restrict__ ops, const void* __restrict__ phase_tab,
         unsigned long long* counters, long long spin_limit) {
   using V = typename P::T;
   using G = typename P::G;
@@ -135,7 +135,7 @@ struct dmv_batch_s {
   int32_t count = 0;
   int32_t precision = DMV_C128;
   int32_t arith = ARITH_FP64;
-  bool fp64_rewrite = true;  // FP64 passes as rotations and phase tables (rewrite_pass_fp64)
+  bool fp64_rewrite = true;  // FP64 passes as rotations and phase tables (rewrite_pass_rotations)
   std::vector<int32_t> n;
   std::vector<std::vector<Gate>> gates;
   std::vector<int64_t> offsets;  // amplitudes
@@ -175,7 +175,9 @@ int batch_plan(dmv_batch_s* b) {
   std::vector<BatchPass> passes;
   std::vector<Op> ops;
   std::vector<PhaseEntry> tab;
-  const bool rewrite = b->precision == DMV_C128 && b->arith == ARITH_FP64 && b->fp64_rewrite;
+  const bool rewrite = b->precision == DMV_C128 && ((b->arith == ARITH_FP64 && b->fp64_rewrite) ||
+                                                     b->arith == ARITH_FP32X2 || b->arith == ARITH_INT64);
+  const bool shears = b->arith == ARITH_FP64;
   std::vector<std::vector<int32_t>> pass_ids((size_t)b->count);
   std::vector<std::vector<int64_t>> pass_tiles((size_t)b->count);
   b->max_k = 0;
@@ -195,7 +197,7 @@ int batch_plan(dmv_batch_s* b) {
       bp.amp_offset = b->offsets[(size_t)c];
       bp.op_begin = (int64_t)ops.size();
       if (rewrite) {
-        bp.num_ops = (int32_t)rewrite_pass_fp64(plan.ops.data() + p.op_begin, p.op_count, bp.k, ops, tab);
+        bp.num_ops = (int32_t)rewrite_pass_rotations(plan.ops.data() + p.op_begin, p.op_count, bp.k, shears, ops, tab);
       } else {
         for (int64_t o = 0; o < p.op_count; ++o) ops.push_back(plan.ops[(size_t)(p.op_begin + o)]);
       }
@@ -253,9 +255,24 @@ int batch_plan(dmv_batch_s* b) {
     DMV_CUDA_TRY(cudaMemcpy(b->items_dev.ptr, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
   if (!ops.empty())
     DMV_CUDA_TRY(cudaMemcpy(b->ops_dev.ptr, ops.data(), ops.size() * sizeof(Op), cudaMemcpyHostToDevice));
-  DMV_TRY(b->phase_tab_dev.reserve(std::max<size_t>(1, tab.size()) * sizeof(PhaseEntry)));
-  if (!tab.empty())
-    DMV_CUDA_TRY(cudaMemcpy(b->phase_tab_dev.ptr, tab.data(), tab.size() * sizeof(PhaseEntry), cudaMemcpyHostToDevice));
+  // The tables in the form the batch's kernel reads: PhaseEntry for FP64 (and
+  // for int64 batches that fall back to FP64), FP32 pairs, or Q.54 limbs.
+  const bool fx = b->arith == ARITH_INT64 && b->all_unitary;
+  const void* src = tab.data();
+  size_t bytes = tab.size() * sizeof(PhaseEntry);
+  std::vector<float4> tdf;
+  std::vector<int4> tfx;
+  if (b->arith == ARITH_FP32X2) {
+    phase_tables_df(tab, tdf);
+    src = tdf.data();
+    bytes = tdf.size() * sizeof(float4);
+  } else if (fx) {
+    phase_tables_fx(tab, tfx);
+    src = tfx.data();
+    bytes = tfx.size() * sizeof(int4);
+  }
+  DMV_TRY(b->phase_tab_dev.reserve(std::max<size_t>(1, bytes)));
+  if (bytes) DMV_CUDA_TRY(cudaMemcpy(b->phase_tab_dev.ptr, src, bytes, cudaMemcpyHostToDevice));
   return DMV_OK;
 }
 
@@ -285,7 +302,7 @@ int batch_launch_kernel(dmv_batch_s* b) {
                                   static_cast<const BatchPass*>(b->passes_dev.ptr),
                                   static_cast<const BatchItem*>(b->items_dev.ptr), b->num_items,
                                   static_cast<const Op*>(b->ops_dev.ptr),
-                                  static_cast<const PhaseEntry*>(b->phase_tab_dev.ptr),
+                                  static_cast<const void*>(b->phase_tab_dev.ptr),
                                   static_cast<unsigned long long*>(b->counters_dev.ptr), b->spin_limit));
   count_launch();
   return DMV_OK;

@@ -114,7 +114,7 @@ inline double cabs(double re, double im) { return std::hypot(re, im); }
 
 // U = D1 R D2 (see the file comment). Returns false when the product does not
 // reproduce U to kZyzTol in every entry.
-bool zyz(const double m[8], double& T, double& S, double& a1, double& a2, double& g2) {
+bool zyz(const double m[8], double& T, double& S, double& C, double& a1, double& a2, double& g2) {
   const double ra = cabs(m[0], m[1]), rb = cabs(m[2], m[3]);
   const double r = std::hypot(ra, rb);
   if (!(r > 0.0)) return false;
@@ -130,6 +130,7 @@ bool zyz(const double m[8], double& T, double& S, double& a1, double& a2, double
     if (!(std::fabs(e[i] - m[i]) <= kZyzTol)) return false;
   T = -s / (1.0 + c);  // -tan(t/2), t = atan2(s, c) in [0, pi/2]
   S = s;
+  C = c;
   return true;
 }
 
@@ -168,8 +169,41 @@ Op blank_op() {
 
 }  // namespace
 
-int64_t rewrite_pass_fp64(const Op* src, int64_t count, int32_t k, std::vector<Op>& dst,
-                          std::vector<PhaseEntry>& tab) {
+// e^{i phi} of an entry in double: i^q (cos phi' + i sin phi') with
+// cos phi' = 1 + s t (t = -tan(phi'/2), s = sin phi').
+void phase_entry_value(const PhaseEntry& e, double& re, double& im) {
+  const double c = 1.0 + e.s * e.t, sn = e.s;
+  const int q = e.swap_xy ? (e.sign_y ? 3 : 1) : (e.sign_x ? 2 : 0);
+  switch (q) {
+    case 0: re = c; im = sn; break;
+    case 1: re = -sn; im = c; break;
+    case 2: re = -c; im = -sn; break;
+    default: re = sn; im = -c; break;
+  }
+}
+
+void phase_tables_df(const std::vector<PhaseEntry>& in, std::vector<float4>& out) {
+  out.resize(in.size());
+  for (size_t i = 0; i < in.size(); ++i) {
+    double re, im;
+    phase_entry_value(in[i], re, im);
+    const float rh = (float)re, ih = (float)im;
+    out[i] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+  }
+}
+
+void phase_tables_fx(const std::vector<PhaseEntry>& in, std::vector<int4>& out) {
+  out.resize(in.size());
+  for (size_t i = 0; i < in.size(); ++i) {
+    double re, im;
+    phase_entry_value(in[i], re, im);
+    const long long fr = std::llround(std::ldexp(re, 54)), fi = std::llround(std::ldexp(im, 54));
+    out[i] = make_int4((int)(fr >> 31), (int)(fr & 0x7FFFFFFFll), (int)(fi >> 31), (int)(fi & 0x7FFFFFFFll));
+  }
+}
+
+int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool shears, std::vector<Op>& dst,
+                               std::vector<PhaseEntry>& tab) {
   const int T = 1 << k;
   std::vector<DiagTable> tables;  // flushes in time order; tables[0] may sit at the pass start
   bool start_table = false;
@@ -223,18 +257,27 @@ int64_t rewrite_pass_fp64(const Op* src, int64_t count, int32_t k, std::vector<O
     }
     if (op.unitary && op.ctrl_kind == CTRL_NONE &&
         (op.cls == OP_GENERAL || op.cls == OP_REAL || op.cls == OP_RXLIKE)) {
-      double Tq, Sq, a1, a2, g2;
-      if (zyz(op.m, Tq, Sq, a1, a2, g2)) {
+      double Tq, Sq, Cq, a1, a2, g2;
+      if (zyz(op.m, Tq, Sq, Cq, a1, a2, g2)) {
         const int t = op.target;
         if (g2 != 0.0) diag(tb, [=](uint32_t l) { return ((l >> t) & 1u) ? g2 : 0.0; });  // D2
         if (pend.supp & tb) flush();
         Op r = blank_op();
-        r.cls = OP_ROT;
         r.target = t;
         r.ctrl = -1;
         r.ctrl_kind = CTRL_NONE;
-        r.m[0] = Tq;
-        r.m[1] = Sq;
+        if (shears) {
+          r.cls = OP_ROT;
+          r.m[0] = Tq;
+          r.m[1] = Sq;
+        } else {  // the rotation as a real 2x2 in the arithmetic's own form
+          r.cls = OP_REAL;
+          r.m[0] = Cq;
+          r.m[2] = -Sq;
+          r.m[4] = Sq;
+          r.m[6] = Cq;
+          split_matrix(r);
+        }
         emit(r);
         // D1: after the rotation on its own bit, so it cannot join an earlier table
         add_term(pend, k, tb, [=](uint32_t l) { return ((l >> t) & 1u) ? a2 : a1; });
@@ -321,7 +364,10 @@ struct Cx {
   double re, im;
 };
 
-void host_op(std::vector<Cx>& tile, int k, const Op& op, const std::vector<PhaseEntry>& tab, uint64_t base) {
+// value_form: apply table entries as the complex value phase_entry_value gives
+// (the form the FP32-pair and int64 kernels read) instead of by shears.
+void host_op(std::vector<Cx>& tile, int k, const Op& op, const std::vector<PhaseEntry>& tab, uint64_t base,
+             bool value_form = false) {
   const uint32_t T = 1u << k;
   if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1u)) return;
   if (op.cls == OP_PHASE) {
@@ -330,6 +376,12 @@ void host_op(std::vector<Cx>& tile, int k, const Op& op, const std::vector<Phase
     for (uint32_t l = 0; l < T; ++l) {
       const PhaseEntry& e = tab[(size_t)op.fh[0] + ((size_t)gsel << k) + l];
       Cx v = tile[l];
+      if (value_form) {
+        double re, im;
+        phase_entry_value(e, re, im);
+        tile[l] = Cx{re * v.re - im * v.im, re * v.im + im * v.re};
+        continue;
+      }
       const double x1 = std::fma(e.t, v.im, v.re);
       const double y1 = std::fma(e.s, x1, v.im);
       const double x2 = std::fma(e.t, y1, x1);
@@ -394,14 +446,17 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
     const int k = ps.low_bits + ps.num_high;
     if (k != 12 || ps.num_high < 3) continue;
     ++n_passes;
+    for (int form = 0; form < 2; ++form) {  // rotations as shears (FP64), then as real 2x2 ops
     std::vector<Op> rw;
     std::vector<PhaseEntry> tab;
-    rewrite_pass_fp64(plan.ops.data() + ps.op_begin, ps.op_count, k, rw, tab);
-    for (const Op& o : rw) {
-      n_rot += o.cls == OP_ROT;
-      n_phase += o.cls == OP_PHASE;
-    }
-    for (int64_t o = 0; o < ps.op_count; ++o) n_general += plan.ops[(size_t)(ps.op_begin + o)].cls != OP_SWAP;
+    rewrite_pass_rotations(plan.ops.data() + ps.op_begin, ps.op_count, k, form == 0, rw, tab);
+    if (form == 0)
+      for (const Op& o : rw) {
+        n_rot += o.cls == OP_ROT;
+        n_phase += o.cls == OP_PHASE;
+      }
+    if (form == 0)
+      for (int64_t o = 0; o < ps.op_count; ++o) n_general += plan.ops[(size_t)(ps.op_begin + o)].cls != OP_SWAP;
     // local bit j of the tile index sits at global qubit pos[j]
     int pos[12];
     for (int j = 0; j < ps.low_bits; ++j) pos[j] = j;
@@ -415,13 +470,14 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
       // the original ops index controls outside the tile by global qubit; the host
       // emulation reads them from `base`, as the kernel does
       for (int64_t o = 0; o < ps.op_count; ++o) host_op(a, k, plan.ops[(size_t)(ps.op_begin + o)], tab, base);
-      for (const Op& o : rw) host_op(b, k, o, tab, base);
+      for (const Op& o : rw) host_op(b, k, o, tab, base, form == 1);
       double num = 0.0, den = 0.0;
       for (size_t i = 0; i < a.size(); ++i) {
         num = std::max(num, std::hypot(a[i].re - b[i].re, a[i].im - b[i].im));
         den = std::max(den, std::hypot(a[i].re, a[i].im));
       }
       worst = std::max(worst, den > 0 ? num / den : num);
+    }
     }
   }
   *max_err = worst;

@@ -61,8 +61,8 @@ enum OpClass : int32_t {
   OP_REAL = 3,     // all four entries real
   OP_ANTI = 4,     // m00 = m11 = 0 (Y and scaled exchanges)
   OP_RXLIKE = 5,   // m00, m11 real and m01, m10 imaginary (RX and its adjoint): 8 multiply-adds
-  // Only in FP64 window passes rewritten by rewrite_pass_fp64 (diag_plan.cpp):
-  OP_ROT = 6,      // real rotation [[c, -s], [s, c]] as three shears: m[0] = -tan(theta/2), m[1] = sin(theta)
+  // Only in window passes rewritten by rewrite_pass_rotations (diag_plan.cpp):
+  OP_ROT = 6,      // FP64: real rotation [[c, -s], [s, c]] as three shears: m[0] = -tan(theta/2), m[1] = sin(theta)
   OP_PHASE = 7     // every amplitude times a phase from a table (PhaseEntry); fields below
 };
 
@@ -157,8 +157,17 @@ void split_matrix(Op& op);
 // rotations on other bits, and earlier into the last table when nothing in
 // between touches its bits. Appends the new ops to `dst` and the tables to
 // `tab`; returns the number of ops appended.
-int64_t rewrite_pass_fp64(const Op* src, int64_t count, int32_t k, std::vector<Op>& dst,
-                          std::vector<PhaseEntry>& tab);
+// `shears` true: rotations as OP_ROT (three shears, the FP64 kernels); false:
+// as OP_REAL 2x2 ops (with their FP32-pair, Q.54 and FP32 forms), for the
+// other arithmetics, which read the tables converted by phase_entry_value.
+int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool shears, std::vector<Op>& dst,
+                               std::vector<PhaseEntry>& tab);
+// e^{i phi} of a table entry in double.
+void phase_entry_value(const PhaseEntry& e, double& re, double& im);
+// The tables in the FP32-pair form (re_h, re_l, im_h, im_l) and as Q.54 limbs
+// (re_h, re_l, im_h, im_l: value = h * 2^31 + l, l in [0, 2^31)).
+void phase_tables_df(const std::vector<PhaseEntry>& in, std::vector<float4>& out);
+void phase_tables_fx(const std::vector<PhaseEntry>& in, std::vector<int4>& out);
 
 // Arithmetic used for complex128 storage.
 enum Arith : int32_t {
@@ -297,8 +306,11 @@ struct dmv_state_s {
   std::vector<dmv::Pass> pass_staging;   // the launches of the last plan (long phase passes split)
   std::vector<dmv::PhaseOp> phase_ops;   // compact ops of the register-phase launches
   dmv::DeviceBuffer phase_ops_dev;
-  std::vector<dmv::PhaseEntry> phase_tab;  // phase tables of the rewritten FP64 passes
+  std::vector<dmv::PhaseEntry> phase_tab;  // phase tables of the rewritten passes
   dmv::DeviceBuffer phase_tab_dev;
+  std::vector<float4> phase_tab_df;        // the same tables for the FP32-pair arithmetic
+  std::vector<int4> phase_tab_fx;          // and for the int64 arithmetic
+  dmv::DeviceBuffer phase_tab2_dev;
   std::vector<dmv::TcStage> tc_stages;  // tensor-core passes of the last plan
   std::vector<uint16_t> tc_u;
   dmv::DeviceBuffer tc_stages_dev, tc_u_dev;

@@ -125,6 +125,7 @@ struct WindowParams {
   int32_t high[16];  // ascending global positions of the high local qubits
   int64_t num_tiles;
   const Op* ops;
+  const void* tab;   // phase tables of the pass's OP_PHASE ops, in the policy's form
 };
 
 static_assert(kWindowThreads == kTileThreads, "tile staging assumes 512 threads");
@@ -147,13 +148,13 @@ k_apply_window(typename P::G* __restrict__ a, const WindowParams p) {
     if constexpr (P::kBlockScaled) {
       const int e = tile_load_fx<false>(tile, a, base, T, t_off, s_slot, s_red);
       __syncthreads();
-      tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base);
+      tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base, p.tab);
       tile_store_fx(tile, a, base, T, t_off, s_slot, e);
     } else {
       (void)s_red;
       tile_load<P, false>(tile, a, base, T, t_off, s_slot);
       __syncthreads();
-      tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base);
+      tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base, p.tab);
       tile_store<P>(tile, a, base, T, t_off, s_slot);
     }
     __syncthreads();
@@ -161,7 +162,8 @@ k_apply_window(typename P::G* __restrict__ a, const WindowParams p) {
 }
 
 template <typename P>
-int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cudaStream_t stream) {
+int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cudaStream_t stream,
+                  const void* tab = nullptr) {
   using V = typename P::T;
   WindowParams p;
   p.k = ps.low_bits + ps.num_high;
@@ -171,6 +173,7 @@ int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cuda
   for (int i = 0; i < 16; ++i) p.high[i] = i < ps.num_high ? ps.high[i] : 0;
   p.num_tiles = int64_t(1) << (n - p.k);
   p.ops = ops_dev + ps.op_begin;
+  p.tab = tab;
   const size_t smem = (size_t(1) << p.k) * sizeof(V);
   static size_t configured = 0;
   if (smem > configured) {
@@ -228,7 +231,7 @@ struct TmaPassParams {
   int64_t num_tiles;
   const Op* ops;
   const PhaseOp* phase_ops;  // k_window_phases' op table (num_ops <= kMaxPhaseOps)
-  const PhaseEntry* phase_tab;  // k_window_tma: tables of the pass's OP_PHASE ops
+  const void* phase_tab;  // k_window_tma: tables of the pass's OP_PHASE ops (PhaseEntry)
   void* amps;        // the statevector (k_window_tma's thread stores)
   int* status;       // set to 1 when a wait gave up
 };
@@ -542,12 +545,12 @@ bool tma_eligible(const Pass& ps) {
 
 template <typename P>
 int launch_window_tma(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, const PhaseOp* phase_ops_dev,
-                      cudaStream_t stream, const PhaseEntry* phase_tab = nullptr) {
+                      cudaStream_t stream, const void* phase_tab = nullptr) {
   if constexpr (!tma_policy<P>()) {
     (void)phase_ops_dev;
-    return launch_window<P>(amps, n, ps, ops_dev, stream);
+    return launch_window<P>(amps, n, ps, ops_dev, stream, phase_tab);
   } else {
-    if (!tma_eligible<P>(ps)) return launch_window<P>(amps, n, ps, ops_dev, stream);
+    if (!tma_eligible<P>(ps)) return launch_window<P>(amps, n, ps, ops_dev, stream, phase_tab);
     constexpr int ES = (int)sizeof(typename P::G);
     constexpr bool PHASES = tma_phases<P>();
     if ((reinterpret_cast<uintptr_t>(amps) & 15u) != 0)
@@ -626,8 +629,8 @@ double op_multiply_adds(const Op& op, int64_t N, int arith) {
     case OP_GENERAL: per_pair = pair_arith ? 172. : fixed ? 64. : 16.; break;
     case OP_RXLIKE: per_pair = pair_arith ? 172. : fixed ? 64. : 8.; break;  // general code in those arithmetics
     case OP_SWAP: per_pair = 0.; break;
-    case OP_ROT: per_pair = 6.; break;    // FP64 only: three shears on re and on im
-    case OP_PHASE: per_pair = 6.; break;  // FP64 only: three shears per amplitude
+    case OP_ROT: per_pair = 6.; break;  // FP64 only: three shears on re and on im
+    case OP_PHASE: per_pair = pair_arith ? 76. : fixed ? 32. : 6.; break;  // one complex product per amplitude
     default: per_pair = pair_arith ? 76. : fixed ? 32. : 8.; break;
   }
   const double pairs = (double)N / 2.0;
@@ -651,17 +654,23 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   ops.assign(plan.ops.begin(), plan.ops.end());
   bool any_window = false, any_phases = false;
   // FP64 window passes on the TMA kernel: rotations and phase tables in place of
-  // general 2x2 ops (rewrite_pass_fp64), appended to the staged ops.
-  const bool rewrite = s->precision == DMV_C128 && s->arith == ARITH_FP64 && s->fp64_rewrite;
+  // general 2x2 ops (rewrite_pass_rotations), appended to the staged ops.
+  // The FP32-pair and int64 arithmetics take the same rewrite with the rotations
+  // as real 2x2 ops and the tables in their own forms.
+  const bool c128 = s->precision == DMV_C128;
+  const bool rewrite = c128 && ((s->arith == ARITH_FP64 && s->fp64_rewrite) || s->arith == ARITH_FP32X2 ||
+                                s->arith == ARITH_INT64);
+  const bool shears = s->arith == ARITH_FP64;
   s->phase_tab.clear();
   for (const Pass& ps : plan.passes) {
     const int rb = ps.kind == 1 ? window_reg_bits(s, ps) : 0;
     any_window |= ps.kind == 1;
-    if (rewrite && ps.kind == 1 && tma_eligible<PolF64>(ps)) {
+    if (rewrite && ps.kind == 1) {
       Pass rw = ps;
       rw.op_begin = (int64_t)ops.size();
       std::vector<Op> src(plan.ops.begin() + ps.op_begin, plan.ops.begin() + ps.op_begin + ps.op_count);
-      rw.op_count = rewrite_pass_fp64(src.data(), ps.op_count, ps.low_bits + ps.num_high, ops, s->phase_tab);
+      rw.op_count =
+          rewrite_pass_rotations(src.data(), ps.op_count, ps.low_bits + ps.num_high, shears, ops, s->phase_tab);
       passes.push_back(rw);
       continue;
     }
@@ -697,12 +706,31 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     phase_ops_dev = static_cast<const PhaseOp*>(s->phase_ops_dev.ptr);
   }
   const Op* ops_dev = static_cast<const Op*>(s->ops_dev.ptr);
-  const PhaseEntry* phase_tab_dev = nullptr;
+  // Phase tables: the FP64 form (also read by an int64 pass that falls back to
+  // FP64) and the FP32-pair or Q.54 form for those arithmetics.
+  const void* phase_tab_dev = nullptr;
+  const void* phase_tab2_dev = nullptr;
+  int64_t tab2_bytes = 0;
   if (!s->phase_tab.empty()) {
     DMV_TRY(s->phase_tab_dev.reserve(s->phase_tab.size() * sizeof(PhaseEntry)));
     DMV_CUDA_TRY(cudaMemcpyAsync(s->phase_tab_dev.ptr, s->phase_tab.data(), s->phase_tab.size() * sizeof(PhaseEntry),
                                  cudaMemcpyHostToDevice, s->stream));
-    phase_tab_dev = static_cast<const PhaseEntry*>(s->phase_tab_dev.ptr);
+    phase_tab_dev = s->phase_tab_dev.ptr;
+    const void* src2 = nullptr;
+    if (s->arith == ARITH_FP32X2) {
+      phase_tables_df(s->phase_tab, s->phase_tab_df);
+      src2 = s->phase_tab_df.data();
+      tab2_bytes = (int64_t)(s->phase_tab_df.size() * sizeof(float4));
+    } else if (s->arith == ARITH_INT64) {
+      phase_tables_fx(s->phase_tab, s->phase_tab_fx);
+      src2 = s->phase_tab_fx.data();
+      tab2_bytes = (int64_t)(s->phase_tab_fx.size() * sizeof(int4));
+    }
+    if (src2) {
+      DMV_TRY(s->phase_tab2_dev.reserve((size_t)tab2_bytes));
+      DMV_CUDA_TRY(cudaMemcpyAsync(s->phase_tab2_dev.ptr, src2, (size_t)tab2_bytes, cudaMemcpyHostToDevice, s->stream));
+      phase_tab2_dev = s->phase_tab2_dev.ptr;
+    }
   }
   // Tensor-core arithmetic: the stages and block digit matrices of every
   // window pass it takes, uploaded once for the whole plan.
@@ -778,8 +806,8 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
       void* a = s->amps;
       cudaStream_t st = s->stream;
       if (s->precision == DMV_C64) DMV_TRY(launch_window_tma<PolF32>(a, s->n, ps, ops_dev, phase_ops_dev, st));
-      else if (arith == ARITH_FP32X2) DMV_TRY(launch_window_tma<PolDF>(a, s->n, ps, ops_dev, phase_ops_dev, st));
-      else if (arith == ARITH_INT64) DMV_TRY(launch_window_tma<PolFX>(a, s->n, ps, ops_dev, phase_ops_dev, st));
+      else if (arith == ARITH_FP32X2) DMV_TRY(launch_window_tma<PolDF>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab2_dev));
+      else if (arith == ARITH_INT64) DMV_TRY(launch_window_tma<PolFX>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab2_dev));
       else DMV_TRY(launch_window_tma<PolF64>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab_dev));
       prof_end(tok, s->stream);
       bytes += 2 * S;
@@ -797,7 +825,7 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   s->last_passes = (int64_t)passes.size();
   s->last_ops = (int64_t)plan.ops.size();
   s->last_phase_tab_bytes = (int64_t)(s->phase_tab.size() * sizeof(PhaseEntry));
-  s->last_upload_bytes = s->last_phase_tab_bytes + (any_window ? (int64_t)(ops.size() * sizeof(Op)) : 0) +
+  s->last_upload_bytes = s->last_phase_tab_bytes + tab2_bytes + (any_window ? (int64_t)(ops.size() * sizeof(Op)) : 0) +
                          (any_phases ? (int64_t)(s->phase_ops.size() * sizeof(PhaseOp)) : 0) +
                          (tc ? (int64_t)(s->tc_stages.size() * sizeof(TcStage) + s->tc_u.size() * 2) : 0);
   s->last_bytes = bytes;

@@ -369,23 +369,86 @@ __device__ __forceinline__ void tile_phase(double2* tile, int T, const Op& op, c
   }
 }
 
+// First table entry of an OP_PHASE op for the tile at `base` (2^k amplitudes).
+__device__ __forceinline__ int64_t phase_slice(const Op& op, int k, int64_t base) {
+  int gsel = 0;
+  for (int j = 0; j < op.fh[1]; ++j) gsel |= (int)((base >> op.fh[2 + j]) & 1) << j;
+  return (int64_t)op.fh[0] + ((int64_t)gsel << k);
+}
+
+// OP_PHASE in FP32-pair arithmetic: amplitude l times the table's pair
+// (re_h, re_l, im_h, im_l), as the diagonal case of df_apply_pair.
+__device__ __forceinline__ void tile_phase_df(float4* tile, int T, const Op& op, const float4* tab, int64_t base) {
+  const float4* e = tab + phase_slice(op, 31 - __clz(T), base);
+  for (int l = threadIdx.x; l < T; l += blockDim.x) {
+    const float4 w = __ldg(e + l);
+    const float4 a = tile[l];
+    DFAcc re, im;
+    df_first(re, w.x, w.y, a.x, a.y);
+    df_add(re, -w.z, -w.w, a.z, a.w);
+    df_first(im, w.x, w.y, a.z, a.w);
+    df_add(im, w.z, w.w, a.x, a.y);
+    float4 b;
+    df_finish(re, b.x, b.y);
+    df_finish(im, b.z, b.w);
+    tile[l] = b;
+  }
+}
+
+// OP_PHASE in int64 block fixed point: amplitude l times the table's Q.54
+// phase (re_h, re_l, im_h, im_l limbs), one rounding per component.
+__device__ __forceinline__ void tile_phase_fx(longlong2* tile, int T, const Op& op, const int4* tab, int64_t base) {
+  const int4* e = tab + phase_slice(op, 31 - __clz(T), base);
+  for (int l = threadIdx.x; l < T; l += blockDim.x) {
+    const int4 w = __ldg(e + l);
+    const longlong2 a = tile[l];
+    int rh, rl, ih, il;
+    fx_limbs(a.x, rh, rl);
+    fx_limbs(a.y, ih, il);
+    FXAcc p, n;
+    fx_zero(p);
+    fx_zero(n);
+    fx_mac(p, w.x, w.y, rh, rl);
+    fx_mac(n, w.z, w.w, ih, il);
+    const long long x = fx_result(p, n);
+    fx_zero(p);
+    fx_mac(p, w.x, w.y, ih, il);
+    fx_mac(p, w.z, w.w, rh, rl);
+    tile[l] = make_longlong2(x, fx_result(p));
+  }
+}
+
 // Every op of a pass on one tile; `base` holds the tile's global index bits
 // (controls outside the tile are read from it). Ends with a barrier after
-// each applied op. `tab` holds the phase tables of OP_PHASE ops (FP64 only).
+// each applied op. `tab` holds the phase tables of OP_PHASE ops in the
+// policy's form: PhaseEntry (FP64), float4 FP32 pairs (PolDF) or int4 Q.54
+// limbs (PolFX).
 template <typename P>
 __device__ __forceinline__ void tile_apply_ops(typename P::T* tile, int T, const Op* ops, int num_ops, int64_t base,
-                                               const PhaseEntry* tab = nullptr) {
+                                               const void* tab = nullptr) {
   for (int o = 0; o < num_ops; ++o) {
     const Op& op = ops[o];
     if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1)) continue;  // uniform per tile
-    if constexpr (std::is_same<typename P::T, double2>::value && std::is_same<typename P::G, double2>::value) {
+    if constexpr (std::is_same<P, PolF64>::value) {
       if (op.cls == OP_ROT) {
         tile_rot(tile, T, op);
         __syncthreads();
         continue;
       }
       if (op.cls == OP_PHASE) {
-        tile_phase(tile, T, op, tab, base);
+        tile_phase(tile, T, op, static_cast<const PhaseEntry*>(tab), base);
+        __syncthreads();
+        continue;
+      }
+    } else if constexpr (std::is_same<P, PolDF>::value) {
+      if (op.cls == OP_PHASE) {
+        tile_phase_df(tile, T, op, static_cast<const float4*>(tab), base);
+        __syncthreads();
+        continue;
+      }
+    } else if constexpr (std::is_same<P, PolFX>::value) {
+      if (op.cls == OP_PHASE) {
+        tile_phase_fx(tile, T, op, static_cast<const int4*>(tab), base);
         __syncthreads();
         continue;
       }

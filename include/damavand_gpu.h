@@ -60,6 +60,8 @@ enum { DMV_C128 = 0, DMV_C64 = 1 };
  *   per-amplitude phase tables, each applied with three more shears.
  * DMV_ARITH_FP64_DIRECT: IEEE FP64 with every fused 2x2 applied as a full
  *   complex multiply-add (8 per amplitude for a general matrix).
+ * The FP32-pair and int64 arithmetics below take the same rotation and phase
+ * table rewrite of their fused passes, with each rotation a real 2x2.
  * DMV_ARITH_FP32X2: the FP64 amplitudes are split into FP32 pairs (about 48
  *   significant bits) inside each kernel and combined with error-free
  *   transformations, then stored back as FP64; GB300 runs FP32 ~71x faster
@@ -297,9 +299,11 @@ int dmv_debug_tc_convert(int32_t mode);
  * DMV_ERR_TIMEOUT. No reference counterpart. */
 int dmv_debug_tma_wait_limit(int64_t polls);
 /* Test hook (host only, no GPU): plans `gates` for num_qubits (12..34) with
- * 2^12-amplitude windows, rewrites every window pass the FP64 TMA kernel takes
- * into rotations and phase tables (DMV_ARITH_FP64), applies the original and
- * the rewritten ops to two random tiles each in host FP64, and returns the
+ * 2^12-amplitude windows, rewrites every window pass into rotations and phase
+ * tables in both forms (rotations as shears and tables by shears, as the FP64
+ * kernels apply them; rotations as real 2x2 ops and tables as complex values,
+ * as the FP32-pair and int64 kernels do), applies the original and the
+ * rewritten ops to two random tiles each in host FP64, and returns the
  * largest normwise difference. counts (may be NULL) receives 4 values: passes
  * checked, non-exchange ops before, rotations and phase tables after. No
  * reference counterpart. */
