@@ -343,8 +343,8 @@ def batch_section(args):
     gates_total = sum(count(g) for _, g in circuits)
     amps = sum(1 << n for n, _ in circuits)
     out, ez = {}, {}
-    runs = [("complex128", "fp64", 16), ("complex128", "fp64-direct", 16), ("complex128", "fp32x2", 16),
-            ("complex128", "int64", 16), ("complex64", "fp32", 8)]
+    runs = [("complex128", "fp64", 16), ("complex128", "fp32x2", 16), ("complex128", "int64", 16),
+            ("complex64", "fp32", 8)]
     for prec, arith, size in runs:
         b = Batch(circuits, prec, "fp64" if prec == "complex64" else arith)
         tune = b.autotune()

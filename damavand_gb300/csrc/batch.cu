@@ -52,8 +52,7 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 template <typename P>
 __global__ void __launch_bounds__(kBatchThreads, 2)
 k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes, const BatchItem* __restrict__ items,
-        int64_t num_items, const Op* __restrict__ ops, const void* __restrict__ phase_tab,
-        unsigned long long* counters, long long spin_limit) {
+        int64_t num_items, const Op* __restrict__ ops, unsigned long long* counters, long long spin_limit) {
   using V = typename P::T;
   using G = typename P::G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -99,12 +98,12 @@ k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes,
       if constexpr (P::kBlockScaled) {
         const int e = tile_load_fx<true>(tile, a, base, T, t_off, s_slot, s_red);
         __syncthreads();
-        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base, phase_tab);
+        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
         tile_store_fx(tile, a, base, T, t_off, s_slot, e);
       } else {
         tile_load<P, true>(tile, a, base, T, t_off, s_slot);
         __syncthreads();
-        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base, phase_tab);
+        tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
         tile_store<P>(tile, a, base, T, t_off, s_slot);
       }
       __syncthreads();
@@ -135,14 +134,13 @@ struct dmv_batch_s {
   int32_t count = 0;
   int32_t precision = DMV_C128;
   int32_t arith = ARITH_FP64;
-  bool fp64_rewrite = true;  // FP64 passes as rotations and phase tables (rewrite_pass_rotations)
   std::vector<int32_t> n;
   std::vector<std::vector<Gate>> gates;
   std::vector<int64_t> offsets;  // amplitudes
   int64_t total_amps = 0;
   void* arena = nullptr;
   cudaStream_t stream = nullptr;
-  DeviceBuffer passes_dev, items_dev, ops_dev, counters_dev, offsets_dev, reduce_dev, phase_tab_dev;
+  DeviceBuffer passes_dev, items_dev, ops_dev, counters_dev, offsets_dev, reduce_dev;
   std::vector<int64_t> red_mass, red_partial, red_sums;  // per-circuit offsets (doubles) into reduce_dev
   int64_t num_items = 0, num_passes = 0, num_ops = 0;
   int32_t max_k = 0;
@@ -174,10 +172,6 @@ void destroy_graph(dmv_batch_s* b) {
 int batch_plan(dmv_batch_s* b) {
   std::vector<BatchPass> passes;
   std::vector<Op> ops;
-  std::vector<PhaseEntry> tab;
-  const bool rewrite = b->precision == DMV_C128 && ((b->arith == ARITH_FP64 && b->fp64_rewrite) ||
-                                                     b->arith == ARITH_FP32X2 || b->arith == ARITH_INT64);
-  const bool shears = b->arith == ARITH_FP64;
   std::vector<std::vector<int32_t>> pass_ids((size_t)b->count);
   std::vector<std::vector<int64_t>> pass_tiles((size_t)b->count);
   b->max_k = 0;
@@ -196,11 +190,7 @@ int batch_plan(dmv_batch_s* b) {
       for (int i = 0; i < p.num_high; ++i) bp.high[i] = p.high[i];
       bp.amp_offset = b->offsets[(size_t)c];
       bp.op_begin = (int64_t)ops.size();
-      if (rewrite) {
-        bp.num_ops = (int32_t)rewrite_pass_rotations(plan.ops.data() + p.op_begin, p.op_count, bp.k, shears, ops, tab);
-      } else {
-        for (int64_t o = 0; o < p.op_count; ++o) ops.push_back(plan.ops[(size_t)(p.op_begin + o)]);
-      }
+      for (int64_t o = 0; o < p.op_count; ++o) ops.push_back(plan.ops[(size_t)(p.op_begin + o)]);
       b->max_k = std::max(b->max_k, bp.k);
       pass_ids[(size_t)c].push_back((int32_t)passes.size());
       pass_tiles[(size_t)c].push_back(int64_t(1) << (b->n[(size_t)c] - bp.k));
@@ -255,24 +245,6 @@ int batch_plan(dmv_batch_s* b) {
     DMV_CUDA_TRY(cudaMemcpy(b->items_dev.ptr, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
   if (!ops.empty())
     DMV_CUDA_TRY(cudaMemcpy(b->ops_dev.ptr, ops.data(), ops.size() * sizeof(Op), cudaMemcpyHostToDevice));
-  // The tables in the form the batch's kernel reads: PhaseEntry for FP64 (and
-  // for int64 batches that fall back to FP64), FP32 pairs, or Q.54 limbs.
-  const bool fx = b->arith == ARITH_INT64 && b->all_unitary;
-  const void* src = tab.data();
-  size_t bytes = tab.size() * sizeof(PhaseEntry);
-  std::vector<float4> tdf;
-  std::vector<int4> tfx;
-  if (b->arith == ARITH_FP32X2) {
-    phase_tables_df(tab, tdf);
-    src = tdf.data();
-    bytes = tdf.size() * sizeof(float4);
-  } else if (fx) {
-    phase_tables_fx(tab, tfx);
-    src = tfx.data();
-    bytes = tfx.size() * sizeof(int4);
-  }
-  DMV_TRY(b->phase_tab_dev.reserve(std::max<size_t>(1, bytes)));
-  if (bytes) DMV_CUDA_TRY(cudaMemcpy(b->phase_tab_dev.ptr, src, bytes, cudaMemcpyHostToDevice));
   return DMV_OK;
 }
 
@@ -302,7 +274,6 @@ int batch_launch_kernel(dmv_batch_s* b) {
                                   static_cast<const BatchPass*>(b->passes_dev.ptr),
                                   static_cast<const BatchItem*>(b->items_dev.ptr), b->num_items,
                                   static_cast<const Op*>(b->ops_dev.ptr),
-                                  static_cast<const void*>(b->phase_tab_dev.ptr),
                                   static_cast<unsigned long long*>(b->counters_dev.ptr), b->spin_limit));
   count_launch();
   return DMV_OK;
@@ -401,8 +372,10 @@ extern "C" int dmv_batch_create(int32_t num_circuits, const int32_t* num_qubits,
   dmv_batch_s* b = new dmv_batch_s();
   b->count = num_circuits;
   b->precision = precision;
+  // Batches apply every fused 2x2 directly: the rotation/phase-table rewrite of
+  // single states builds one table per pass, which many small circuits cannot
+  // amortise (config-4-like batches: ~22k tables, 2.9 GB, for 512 circuits).
   b->arith = arithmetic == DMV_ARITH_FP64_DIRECT ? (int32_t)ARITH_FP64 : arithmetic;
-  b->fp64_rewrite = arithmetic == DMV_ARITH_FP64;
   int64_t off = 0;
   for (int32_t c = 0; c < num_circuits; ++c) {
     const int32_t n = num_qubits[c];

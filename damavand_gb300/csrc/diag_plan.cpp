@@ -45,7 +45,17 @@ constexpr double kTwoPi = 6.283185307179586476925286766559;
 constexpr double kHalfPi = 1.5707963267948966192313216916398;
 constexpr double kZyzTol = 4e-15;  // per entry, about 18 ulp of 1
 
+constexpr double kPi = 3.1415926535897932384626433832795;
+
 inline double wrap(double a) { return std::remainder(a, kTwoPi); }
+
+// x + a reduced to [-pi, pi] for x, a in [-pi, pi] (every term angle is).
+inline double add_angle(double x, double a) {
+  x += a;
+  if (x > kPi) x -= kTwoPi;
+  else if (x < -kPi) x += kTwoPi;
+  return x;
+}
 
 // A diagonal phase over the tile (2^k amplitudes) and up to kMaxPhaseGlobals
 // global bits: angle of amplitude l on tiles with global-bit pattern gsel at
@@ -64,15 +74,30 @@ struct DiagTable {
   }
 };
 
-// Adds the phase f(l) of one diagonal factor (local bits only) to every slice.
+// Adds the phase f(l) of one diagonal factor (local bits only, |f| <= pi) to every slice.
 template <typename F>
 void add_term(DiagTable& d, int k, uint32_t bits, F f) {
   const size_t T = size_t(1) << k;
+  double* a = d.ang.data();
   for (size_t idx = 0; idx < d.ang.size(); ++idx) {
-    const double a = f((uint32_t)(idx & (T - 1)));
-    if (a != 0.0) d.ang[idx] = wrap(d.ang[idx] + a);
+    const double v = f((uint32_t)(idx & (T - 1)));
+    if (v != 0.0) a[idx] = add_angle(a[idx], v);
   }
   d.supp |= bits;
+  d.used = true;
+}
+
+// The same for a factor on one bit t: p0 where the bit is clear, p1 where it is set.
+void add_bit_term(DiagTable& d, int t, double p0, double p1) {
+  const size_t n = d.ang.size(), tb = size_t(1) << t;
+  double* a = d.ang.data();
+  for (size_t base = 0; base < n; base += 2 * tb) {
+    if (p0 != 0.0)
+      for (size_t i = base; i < base + tb; ++i) a[i] = add_angle(a[i], p0);
+    if (p1 != 0.0)
+      for (size_t i = base + tb; i < base + 2 * tb; ++i) a[i] = add_angle(a[i], p1);
+  }
+  d.supp |= 1u << t;
   d.used = true;
 }
 
@@ -81,14 +106,17 @@ void add_term(DiagTable& d, int k, uint32_t bits, F f) {
 bool permute(DiagTable& d, int k, const Op& op) {
   const uint32_t tb = 1u << op.target;
   if (!(d.supp & tb)) return true;  // does not depend on the target: unchanged
-  const size_t T = size_t(1) << k;
-  std::vector<double> old = d.ang;
+  // the exchange is an involution: swap the entries of each pair it maps onto each other
+  double* a = d.ang.data();
+  const size_t n = d.ang.size();
   if (op.ctrl_kind == CTRL_NONE) {
-    for (size_t idx = 0; idx < old.size(); ++idx) d.ang[idx] = old[idx ^ tb];
+    for (size_t idx = 0; idx < n; ++idx)
+      if (!(idx & tb)) std::swap(a[idx], a[idx | tb]);
   } else if (op.ctrl_kind == CTRL_LOCAL) {
-    const int c = op.ctrl;
-    for (size_t idx = 0; idx < old.size(); ++idx) d.ang[idx] = old[idx ^ (((idx >> c) & 1u) ? tb : 0u)];
-    d.supp |= 1u << c;
+    const size_t cb = size_t(1) << op.ctrl;
+    for (size_t idx = 0; idx < n; ++idx)
+      if (!(idx & tb) && (idx & cb)) std::swap(a[idx], a[idx | tb]);
+    d.supp |= 1u << op.ctrl;
   } else {
     int j = -1;
     for (int i = 0; i < d.g; ++i)
@@ -97,15 +125,14 @@ bool permute(DiagTable& d, int k, const Op& op) {
       if (d.g == kMaxPhaseGlobals) return false;
       j = d.g++;
       d.gq[j] = op.ctrl;
-      d.ang.resize(old.size() * 2);
-      std::memcpy(d.ang.data() + old.size(), old.data(), old.size() * sizeof(double));
-      old = d.ang;
+      const size_t old = d.ang.size();
+      d.ang.resize(old * 2);
+      std::memcpy(d.ang.data() + old, d.ang.data(), old * sizeof(double));
     }
-    for (size_t idx = 0; idx < old.size(); ++idx) {
-      const bool on = ((idx >> k) >> j) & 1u;
-      d.ang[idx] = on ? old[idx ^ tb] : old[idx];
-    }
-    (void)T;
+    a = d.ang.data();
+    const size_t on = size_t(1) << (k + j);
+    for (size_t idx = 0; idx < d.ang.size(); ++idx)
+      if ((idx & on) && !(idx & tb)) std::swap(a[idx], a[idx | tb]);
   }
   return true;
 }
@@ -143,9 +170,10 @@ PhaseEntry entry_of(double phi) {
   const double p = phi - qf * kHalfPi;
   const int q = (((int)qf % 4) + 4) % 4;
   PhaseEntry e;
-  const double h = 0.5 * p;
-  e.t = -std::tan(h);
-  e.s = std::sin(p);
+  double sh, ch;
+  sincos(0.5 * p, &sh, &ch);  // t = -tan(p/2), s = sin p = 2 sin(p/2) cos(p/2)
+  e.t = -sh / ch;
+  e.s = 2.0 * sh * ch;
   e.swap_xy = (uint32_t)(q & 1);
   e.sign_x = (q == 1 || q == 2) ? 0x80000000u : 0u;
   e.sign_y = (q == 2 || q == 3) ? 0x80000000u : 0u;
@@ -239,6 +267,22 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool she
       add_term(pend, k, bits, f);
     }
   };
+  // The same for a factor on one bit t (p0 where clear, p1 where set).
+  auto diag_bit = [&](int t, double p0, double p1) {
+    const uint32_t bits = 1u << t;
+    if (!(bits & touched)) {
+      if (last < 0) {
+        DiagTable d;
+        d.reset(T);
+        tables.insert(tables.begin(), d);
+        start_table = true;
+        last = 0;
+      }
+      add_bit_term(tables[(size_t)last], t, p0, p1);
+    } else {
+      add_bit_term(pend, t, p0, p1);
+    }
+  };
   auto emit = [&](const Op& op) {
     items.push_back(Item{false, -1, op});
     touched |= 1u << op.target;
@@ -260,7 +304,7 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool she
       double Tq, Sq, Cq, a1, a2, g2;
       if (zyz(op.m, Tq, Sq, Cq, a1, a2, g2)) {
         const int t = op.target;
-        if (g2 != 0.0) diag(tb, [=](uint32_t l) { return ((l >> t) & 1u) ? g2 : 0.0; });  // D2
+        if (g2 != 0.0) diag_bit(t, 0.0, g2);  // D2
         if (pend.supp & tb) flush();
         Op r = blank_op();
         r.target = t;
@@ -280,7 +324,7 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool she
         }
         emit(r);
         // D1: after the rotation on its own bit, so it cannot join an earlier table
-        add_term(pend, k, tb, [=](uint32_t l) { return ((l >> t) & 1u) ? a2 : a1; });
+        add_bit_term(pend, t, a1, a2);
         continue;
       }
     }
@@ -289,7 +333,7 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool she
       const int t = op.target;
       const double p0 = std::atan2(op.m[1], op.m[0]), p1 = std::atan2(op.m[7], op.m[6]);
       if (op.ctrl_kind == CTRL_NONE) {
-        diag(tb, [=](uint32_t l) { return ((l >> t) & 1u) ? p1 : p0; });
+        diag_bit(t, p0, p1);
       } else {
         const int c = op.ctrl;
         diag(tb | (1u << c), [=](uint32_t l) { return ((l >> c) & 1u) ? (((l >> t) & 1u) ? p1 : p0) : 0.0; });
@@ -301,7 +345,7 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool she
       // [[0, b], [c, 0]] = X diag(c, b)
       const int t = op.target;
       const double pc = std::atan2(op.m[5], op.m[4]), pb = std::atan2(op.m[3], op.m[2]);
-      diag(tb, [=](uint32_t l) { return ((l >> t) & 1u) ? pb : pc; });
+      diag_bit(t, pc, pb);
       Op x = blank_op();
       x.cls = OP_SWAP;
       x.target = t;
@@ -339,7 +383,7 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool she
     p.fh[0] = (int32_t)tab.size();
     p.fh[1] = d.g;
     for (int j = 0; j < d.g; ++j) p.fh[2 + j] = d.gq[j];
-    tab.reserve(tab.size() + d.ang.size());
+    if (tab.capacity() < tab.size() + d.ang.size()) tab.reserve(2 * (tab.size() + d.ang.size()));
     for (double a : d.ang) tab.push_back(entry_of(a));
     dst.push_back(p);
   };

@@ -77,7 +77,8 @@ enum { DMV_C128 = 0, DMV_C64 = 1 };
  *   (7 per 56-bit integer, FP16) on the tensor cores (tcgen05.mma, FP32
  *   accumulators in tensor memory, every sum exact), rounded once per
  *   output. Passes it does not take run as DMV_ARITH_INT64. Single states
- *   only (batches accept FP64, FP64_DIRECT, FP32X2 and INT64). */
+ *   only (batches accept FP64, FP64_DIRECT, FP32X2 and INT64; a batch applies
+ *   every fused 2x2 directly, as DMV_ARITH_FP64_DIRECT does). */
 enum { DMV_ARITH_FP64 = 0, DMV_ARITH_FP32X2 = 1, DMV_ARITH_INT64 = 2, DMV_ARITH_TC = 3, DMV_ARITH_FP64_DIRECT = 4 };
 
 /* Gate kinds (numbering shared with the oracle). DMV_GATE_MATRIX takes an
