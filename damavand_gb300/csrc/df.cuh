@@ -37,15 +37,20 @@ __device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
   }
   const unsigned int m23 = (unsigned int)(b >> 29) & 0x7FFFFFu;
   hi = __uint_as_float(sign | ((unsigned int)ef << 23) | m23);
-  // lo = r * 2^(E - 1075), r the low 29 mantissa bits. 2^(E-1075) is a normal
-  // float only for E >= 949; below that the weight is applied in two factors
-  // (2^-64 and 2^(E-1011), both normal for 897 <= E < 949), so lo keeps its 24
-  // bits while it stays in FP32's normal range (|x| >= 2^-102).
+  // lo = r * 2^(E - 1075), r the low 29 mantissa bits, rounded to 24 bits.
+  // No conversion instruction (those run at the FP64 rate): with r = 64 rh + rl,
+  // rh * 2^-23 = bits(1.0f | rh) - 1 and rl = bits(2^23 | rl) - 2^23 are exact,
+  // and one FMA forms r * 2^-29 rounded to nearest even (the same value as
+  // converting r). The weight 2^(E - 1046) is a normal float for E >= 920; below
+  // that it is applied in two factors (2^-64 and 2^(E - 982)), so lo keeps its
+  // 24 bits while it stays in FP32's normal range (|x| >= 2^-102).
   const unsigned int r = (unsigned int)b & 0x1FFFFFFFu;
-  const float rf = __uint2float_rn(r);
+  const float fh = __fsub_rn(__uint_as_float(0x3F800000u | (r >> 6)), 1.0f);
+  const float fl = __fsub_rn(__uint_as_float(0x4B000000u | (r & 63u)), 8388608.0f);
+  const float u = __fmaf_rn(fl, 0x1p-29f, fh);
   float l;
-  if (E >= 949) l = __fmul_rn(rf, __uint_as_float((unsigned int)(E - 948) << 23));
-  else l = __fmul_rn(__fmul_rn(rf, 0x1p-64f), __uint_as_float((unsigned int)(E - 884) << 23));
+  if (E >= 920) l = __fmul_rn(u, __uint_as_float((unsigned int)(E - 919) << 23));
+  else l = __fmul_rn(__fmul_rn(u, 0x1p-64f), __uint_as_float((unsigned int)(E - 855) << 23));
   lo = __uint_as_float(__float_as_uint(l) | sign);
 }
 

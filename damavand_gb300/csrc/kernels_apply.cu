@@ -130,7 +130,12 @@ struct WindowParams {
 
 static_assert(kWindowThreads == kTileThreads, "tile staging assumes 512 threads");
 
-template <typename P>
+// FMT (FP32-pair arithmetic only): bit 0, the pass reads the FP32-pair form
+// (float4 in place of each double2, the same 16 bytes); bit 1, it writes that
+// form. Inside one gate list of window passes only the first pass reads IEEE
+// complex128 and only the last one writes it, so the passes between skip the
+// integer-heavy conversions.
+template <typename P, int FMT = 0>
 __global__ void __launch_bounds__(kWindowThreads, 2)
 k_apply_window(typename P::G* __restrict__ a, const WindowParams p) {
   using V = typename P::T;
@@ -152,18 +157,20 @@ k_apply_window(typename P::G* __restrict__ a, const WindowParams p) {
       tile_store_fx(tile, a, base, T, t_off, s_slot, e);
     } else {
       (void)s_red;
-      tile_load<P, false>(tile, a, base, T, t_off, s_slot);
+      if constexpr (FMT & 1) tile_load<PolRaw<P>, false>(tile, reinterpret_cast<const V*>(a), base, T, t_off, s_slot);
+      else tile_load<P, false>(tile, a, base, T, t_off, s_slot);
       __syncthreads();
       tile_apply_ops<P>(tile, T, p.ops, p.num_ops, base, p.tab);
-      tile_store<P>(tile, a, base, T, t_off, s_slot);
+      if constexpr (FMT & 2) tile_store<PolRaw<P>>(tile, reinterpret_cast<V*>(a), base, T, t_off, s_slot);
+      else tile_store<P>(tile, a, base, T, t_off, s_slot);
     }
     __syncthreads();
   }
 }
 
-template <typename P>
-int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cudaStream_t stream,
-                  const void* tab = nullptr) {
+template <typename P, int FMT>
+int launch_window_fmt(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cudaStream_t stream,
+                      const void* tab) {
   using V = typename P::T;
   WindowParams p;
   p.k = ps.low_bits + ps.num_high;
@@ -177,16 +184,31 @@ int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cuda
   const size_t smem = (size_t(1) << p.k) * sizeof(V);
   static size_t configured = 0;
   if (smem > configured) {
-    DMV_CUDA_TRY(cudaFuncSetAttribute(k_apply_window<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    DMV_CUDA_TRY(cudaFuncSetAttribute(k_apply_window<P, FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)std::max<size_t>(smem, 48 * 1024)));
     configured = smem;
   }
   int per_sm = 0;
-  DMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_window<P>, kWindowThreads, smem));
+  DMV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_window<P, FMT>, kWindowThreads, smem));
   if (per_sm < 1) return set_error(DMV_ERR_CUDA, "window kernel cannot fit %zu bytes of shared memory", smem);
   const int64_t grid = std::min<int64_t>(p.num_tiles, (int64_t)per_sm * num_sms());
-  k_apply_window<P><<<(int)grid, kWindowThreads, smem, stream>>>(static_cast<typename P::G*>(amps), p);
+  k_apply_window<P, FMT><<<(int)grid, kWindowThreads, smem, stream>>>(static_cast<typename P::G*>(amps), p);
   return DMV_OK;
+}
+
+// fmt: the FMT bits of k_apply_window (FP32-pair arithmetic only).
+template <typename P>
+int launch_window(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, cudaStream_t stream,
+                  const void* tab = nullptr, int fmt = 0) {
+  if constexpr (std::is_same<P, PolDF>::value) {
+    switch (fmt) {
+      case 1: return launch_window_fmt<P, 1>(amps, n, ps, ops_dev, stream, tab);
+      case 2: return launch_window_fmt<P, 2>(amps, n, ps, ops_dev, stream, tab);
+      case 3: return launch_window_fmt<P, 3>(amps, n, ps, ops_dev, stream, tab);
+      default: break;
+    }
+  }
+  return launch_window_fmt<P, 0>(amps, n, ps, ops_dev, stream, tab);
 }
 
 // ---------------------------------------------------------------------------
@@ -545,11 +567,12 @@ bool tma_eligible(const Pass& ps) {
 
 template <typename P>
 int launch_window_tma(void* amps, int32_t n, const Pass& ps, const Op* ops_dev, const PhaseOp* phase_ops_dev,
-                      cudaStream_t stream, const void* phase_tab = nullptr) {
+                      cudaStream_t stream, const void* phase_tab = nullptr, int fmt = 0) {
   if constexpr (!tma_policy<P>()) {
     (void)phase_ops_dev;
-    return launch_window<P>(amps, n, ps, ops_dev, stream, phase_tab);
+    return launch_window<P>(amps, n, ps, ops_dev, stream, phase_tab, fmt);
   } else {
+    (void)fmt;
     if (!tma_eligible<P>(ps)) return launch_window<P>(amps, n, ps, ops_dev, stream, phase_tab);
     constexpr int ES = (int)sizeof(typename P::G);
     constexpr bool PHASES = tma_phases<P>();
@@ -766,8 +789,13 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   }
   int64_t bytes = 0;
   const int64_t S = (int64_t)s->amp_bytes();
+  // FP32-pair arithmetic: when every launch is a window pass, the state stays in
+  // the FP32-pair form between them (k_apply_window's FMT bits).
+  bool df_chain = c128 && s->arith == ARITH_FP32X2 && passes.size() >= 2;
+  for (const Pass& ps : passes) df_chain = df_chain && ps.kind == 1;
   for (size_t pi = 0; pi < passes.size(); ++pi) {
     const Pass& ps = passes[pi];
+    const int df_fmt = df_chain ? ((pi > 0 ? 1 : 0) | (pi + 1 < passes.size() ? 2 : 0)) : 0;
     if (tc && tc_first[pi] >= 0) {
       // Tensor-core FLOPs: 34 digit products of a 128 x 64 x 64 real product per
       // 4096-amplitude tile and block (2 FLOPs per multiply-add).
@@ -806,7 +834,8 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
       void* a = s->amps;
       cudaStream_t st = s->stream;
       if (s->precision == DMV_C64) DMV_TRY(launch_window_tma<PolF32>(a, s->n, ps, ops_dev, phase_ops_dev, st));
-      else if (arith == ARITH_FP32X2) DMV_TRY(launch_window_tma<PolDF>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab2_dev));
+      else if (arith == ARITH_FP32X2)
+        DMV_TRY(launch_window_tma<PolDF>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab2_dev, df_fmt));
       else if (arith == ARITH_INT64) DMV_TRY(launch_window_tma<PolFX>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab2_dev));
       else DMV_TRY(launch_window_tma<PolF64>(a, s->n, ps, ops_dev, phase_ops_dev, st, phase_tab_dev));
       prof_end(tok, s->stream);

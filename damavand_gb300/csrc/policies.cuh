@@ -114,6 +114,18 @@ struct PolFX {
   __device__ static G out(const T& t, int e) { return make_double2(fx_to_double(t.x, e), fx_to_double(t.y, e)); }
 };
 
+// Staging view of a policy whose working type is already the HBM contents:
+// the tile is loaded and stored without conversion (FP32-pair passes between
+// the first and last of a gate list keep that form in HBM).
+template <typename P>
+struct PolRaw {
+  static constexpr bool kBlockScaled = false;
+  using G = typename P::T;
+  using T = typename P::T;
+  __device__ static T in(const G& g) { return g; }
+  __device__ static G out(const T& t) { return t; }
+};
+
 // (a0, a1) <- M (a0, a1) with the op class chosen at run time.
 template <typename P>
 __device__ __forceinline__ void apply_dyn(int cls, const typename P::Mat& m, typename P::T& a0, typename P::T& a1) {
