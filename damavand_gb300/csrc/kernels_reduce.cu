@@ -261,19 +261,19 @@ k_chunk_mass_f2(const void* src, int n, int chunk_bits, int64_t num_chunks, doub
         if ((ch >> j) & 1) hi_acc[j] += t;
     }
   }
-  double T = 0.;
-  double R[4] = {0., 0., 0., 0.};
+  // fold the rows in FP32 pairs (FP64 only for the five results)
+  F2 T{0.f, 0.f};
+  F2 R[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
   for (int r = 0; r < kF2Rows; ++r) {
-    const double x = f2_val(v[r]);
-    T += x;
+    f2_add(T, v[r].h, v[r].l);
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      if ((r >> j) & 1) R[j] += x;
+      if ((r >> j) & 1) f2_add(R[j], v[r].h, v[r].l);
   }
-  tsum[threadIdx.x] = T;
+  tsum[threadIdx.x] = f2_val(T);
 #pragma unroll
-  for (int j = 0; j < 4; ++j) rsum[j][threadIdx.x] = R[j];
+  for (int j = 0; j < 4; ++j) rsum[j][threadIdx.x] = f2_val(R[j]);
   __syncthreads();
   double* out = partial + (int64_t)blockIdx.x * (n + 1);
   const int q = threadIdx.x;
@@ -673,6 +673,11 @@ k_adjoint_step(typename P::G* __restrict__ psi, typename P::G* __restrict__ lam,
 int chunk_bits_for(int n) { return std::min(kMaxChunkBits, n); }
 // Chunks of the Pauli-Z mass pass (k_chunk_mass_f2): 4096 amplitudes.
 int mass_chunk_bits_for(int n) { return std::min(kF2ChunkBits, n); }
+// Its grid: two CTAs per SM, each striding over many chunks, so the per-CTA
+// fold at the end (per-bit sums over the threads) is amortised.
+int mass_grid_for_chunks(int64_t num_chunks) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(num_chunks, (int64_t)sm_count() * 2));
+}
 
 // The per-chunk / per-bit mass pass: FP32 pairs for amplitudes (src_kind 0
 // complex128, 1 complex64), FP64 for a probability vector (src_kind 2).
@@ -696,7 +701,7 @@ int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& chunk_de
                     int64_t* num_chunks_out, int* chunk_bits_out) {
   const int cb = src_kind == 2 ? chunk_bits_for(n) : mass_chunk_bits_for(n);
   const int64_t num_chunks = int64_t(1) << (n - cb);
-  const int grid = grid_for_chunks(num_chunks);
+  const int grid = src_kind == 2 ? grid_for_chunks(num_chunks) : mass_grid_for_chunks(num_chunks);
   DMV_TRY(chunk_dev.reserve((size_t)num_chunks * sizeof(double)));
   const size_t partial_elems = (size_t)grid * (n + 1);
   DMV_TRY(reduce_dev.reserve((partial_elems + (size_t)(n + 1)) * sizeof(double)));
@@ -788,7 +793,7 @@ ChunkMassShape chunk_mass_shape(int n) {
   ChunkMassShape sh;
   sh.chunk_bits = mass_chunk_bits_for(n);
   sh.num_chunks = int64_t(1) << (n - sh.chunk_bits);
-  sh.grid = grid_for_chunks(sh.num_chunks);
+  sh.grid = mass_grid_for_chunks(sh.num_chunks);
   sh.partial_elems = (int64_t)sh.grid * (n + 1);
   return sh;
 }
