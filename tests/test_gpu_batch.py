@@ -56,7 +56,8 @@ def test_batch_complex64_reports_error_against_complex128(built_lib, oracle_mod)
 
 
 def test_batch_config4_shape_runs_and_checks_a_sample(built_lib, oracle_mod):
-    """The full 512-circuit, 10..22-qubit, depth 5..40 batch; oracle check on the smallest circuits."""
+    """The full 512-circuit, 10..22-qubit, depth 5..40 batch; oracle check on the six smallest
+    circuits and on the two largest 22-qubit ones (the oracle in its in-place mode)."""
     from damavand_gb300.batch import Batch
     from damavand_gb300.workloads import uneven_batch
     circuits = uneven_batch(512, seed=4)
@@ -64,10 +65,14 @@ def test_batch_config4_shape_runs_and_checks_a_sample(built_lib, oracle_mod):
     ms = b.run()
     assert ms > 0
     ez = b.expect_z()
-    order = np.argsort([n for n, _ in circuits])[:6]
+    sizes = np.array([n for n, _ in circuits])
+    depth = np.array([len(g) for _, g in circuits])
+    big = [int(i) for i in np.flatnonzero(sizes == sizes.max())]
+    big = sorted(big, key=lambda i: -depth[i])[:2]
+    order = list(np.argsort(sizes)[:6]) + big
     for i in order:
         n, gates = circuits[i]
-        want = oracle_mod.forward(n, gates)
+        want = oracle_mod.forward(n, gates, clone=False)
         assert_state_close(b.state(int(i)), want, what=f"circuit {i}")
         assert np.max(np.abs(ez[i] - oracle_mod.expect_z(oracle_mod.measure(want)))) <= EXPECT_ATOL
 
