@@ -32,6 +32,8 @@ struct BatchPass {
   int32_t high[16];
   int64_t amp_offset;  // first amplitude of the circuit in the arena
   int64_t op_begin;    // first op in the batch op array
+  int32_t fmt;         // FP32-pair batches: bit 0 reads, bit 1 writes the pair form (not its
+  int32_t pad;         // circuit's first / last pass), so the passes between skip the conversions
 };
 
 struct BatchItem {
@@ -101,10 +103,20 @@ k_batch(typename P::G* __restrict__ arena, const BatchPass* __restrict__ passes,
         tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
         tile_store_fx(tile, a, base, T, t_off, s_slot, e);
       } else {
-        tile_load<P, true>(tile, a, base, T, t_off, s_slot);
+        if constexpr (std::is_same<P, PolDF>::value) {
+          if (ps.fmt & 1) tile_load<PolRaw<P>, true>(tile, reinterpret_cast<const V*>(a), base, T, t_off, s_slot);
+          else tile_load<P, true>(tile, a, base, T, t_off, s_slot);
+        } else {
+          tile_load<P, true>(tile, a, base, T, t_off, s_slot);
+        }
         __syncthreads();
         tile_apply_ops<P>(tile, T, ops + ps.op_begin, ps.num_ops, base);
-        tile_store<P>(tile, a, base, T, t_off, s_slot);
+        if constexpr (std::is_same<P, PolDF>::value) {
+          if (ps.fmt & 2) tile_store<PolRaw<P>>(tile, reinterpret_cast<V*>(a), base, T, t_off, s_slot);
+          else tile_store<P>(tile, a, base, T, t_off, s_slot);
+        } else {
+          tile_store<P>(tile, a, base, T, t_off, s_slot);
+        }
       }
       __syncthreads();
     }
@@ -192,6 +204,10 @@ int batch_plan(dmv_batch_s* b) {
       bp.op_begin = (int64_t)ops.size();
       for (int64_t o = 0; o < p.op_count; ++o) ops.push_back(plan.ops[(size_t)(p.op_begin + o)]);
       b->max_k = std::max(b->max_k, bp.k);
+      if (b->precision == DMV_C128 && b->arith == ARITH_FP32X2) {
+        const size_t pi = (size_t)(&p - plan.passes.data());
+        bp.fmt = (pi > 0 ? 1 : 0) | (pi + 1 < plan.passes.size() ? 2 : 0);
+      }
       pass_ids[(size_t)c].push_back((int32_t)passes.size());
       pass_tiles[(size_t)c].push_back(int64_t(1) << (b->n[(size_t)c] - bp.k));
       passes.push_back(bp);
