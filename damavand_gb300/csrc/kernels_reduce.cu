@@ -675,7 +675,9 @@ int chunk_bits_for(int n) { return std::min(kMaxChunkBits, n); }
 int mass_chunk_bits_for(int n) { return std::min(kF2ChunkBits, n); }
 // Its grid: eight CTAs per SM (two CTAs per SM measured 1.4x slower: too few
 // loads in flight).
-int mass_grid_for_chunks(int64_t num_chunks) { return grid_for_chunks(num_chunks); }
+int mass_grid_for_chunks(int64_t num_chunks) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(num_chunks, (int64_t)sm_count() * 8));
+}
 
 // The per-chunk / per-bit mass pass: FP32 pairs for amplitudes (src_kind 0
 // complex128, 1 complex64), FP64 for a probability vector (src_kind 2).
