@@ -540,6 +540,8 @@ extern "C" int dmv_batch_autotune(dmv_batch_t b, int32_t* tile_bits, int32_t* lo
 extern "C" int dmv_batch_expect_z(dmv_batch_t b, double* out) {
   clear_error();
   if (!b || !out) return set_error(DMV_ERR_INVALID, "null batch or output");
+  DMV_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  DMV_TRY(check_window_status());  // a mass pass whose chunk load wait gave up
   int64_t pos = 0;
   for (int32_t c = 0; c < b->count; ++c) {
     const int n = b->n[(size_t)c];

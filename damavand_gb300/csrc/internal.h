@@ -358,11 +358,15 @@ int launch_adjoint_step(dmv_state_s* psi, dmv_state_s* lam, const Op& op, double
 int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const double* weights,
                      double* loss, double* grads);
 int upload_ops(dmv_state_s* s, const Op* ops, int64_t count);
-// DMV_ERR_TIMEOUT (and clears the flag) when a TMA window pass gave up
-// waiting for a tile load since the last check; synchronises the device.
+// DMV_ERR_TIMEOUT (and clears the flag) when a TMA window pass or the
+// bulk-staged chunk-mass pass gave up waiting for a load since the last
+// check; synchronises the device.
 int check_window_status();
-// Polls before a TMA tile-load wait gives up; negative restores the default.
+// Polls before a TMA load wait gives up; negative restores the default.
 void set_tma_wait_limit(int64_t polls);
+uint32_t tma_wait_limit();
+// The device word those waits set to 1 when they give up.
+int* tma_status_word();
 
 // Chunk-mass / Pauli-Z reduction into caller-provided device buffers:
 // `mass` holds num_chunks doubles, `partial` partial_elems, `sums` n+1

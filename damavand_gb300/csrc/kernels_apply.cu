@@ -875,8 +875,9 @@ int launch_set_zero(dmv_state_s* s) {
   return DMV_OK;
 }
 
-// A load wait of the TMA window kernel that gave up leaves 1 in the
-// device status word; report it (and clear it) as DMV_ERR_TIMEOUT.
+// A load wait of a TMA window kernel or of the bulk-staged chunk-mass pass
+// that gave up leaves 1 in the device status word; report it (and clear it)
+// as DMV_ERR_TIMEOUT.
 int check_window_status() {
   int* p = tma_status_ptr();
   if (!p) return DMV_OK;
@@ -885,10 +886,13 @@ int check_window_status() {
   if (v != 0) {
     const int zero = 0;
     DMV_CUDA_TRY(cudaMemcpy(p, &zero, sizeof(int), cudaMemcpyHostToDevice));
-    return set_error(DMV_ERR_TIMEOUT, "a TMA tile load did not complete within its wait limit");
+    return set_error(DMV_ERR_TIMEOUT, "a TMA load did not complete within its wait limit");
   }
   return DMV_OK;
 }
+
+int* tma_status_word() { return tma_status_ptr(); }
+uint32_t tma_wait_limit() { return g_tma_wait_limit; }
 
 void set_tma_wait_limit(int64_t polls) {
   g_tma_wait_limit = polls < 0 ? kTmaWaitLimit : (uint32_t)std::min<int64_t>(polls, 0xffffffffLL);

@@ -14,6 +14,7 @@
 #include "df.cuh"
 #include "internal.h"
 #include "policies.cuh"
+#include "tma.cuh"
 
 namespace dmv {
 
@@ -296,6 +297,297 @@ k_chunk_mass_f2(const void* src, int n, int chunk_bits, int64_t num_chunks, doub
 }
 static_assert((1 << kF2ChunkBits) == kRedThreads * kF2Rows, "a chunk is one amplitude per thread and row");
 static_assert(kF2ChunkBits < kRedThreads - 1, "the total's thread is not a per-bit thread");
+
+// ---------------------------------------------------------------------------
+// k_chunk_mass_bulk: the same pass for states of 12 or more qubits, with one
+// CTA per SM and the chunks staged in shared memory by the copy engine.
+//
+// The register-fed pass above keeps too few loads in flight per SM for HBM
+// speed (its grid sweep: two CTAs per SM ran at a quarter of HBM bandwidth,
+// eight at about half). Here one thread starts an untiled bulk copy
+// (cp.async.bulk) per 4096-amplitude chunk into a ring of three buffers, so
+// two chunks (128 KB of complex128) are in flight while the third is summed,
+// whatever the register count. The arithmetic is cut to about 60 operations
+// per amplitude (split47 below, a TwoSum in place of a full pair addition for
+// |x|^2 + |y|^2). Each thread owns 8 amplitudes of a chunk (elements
+// tid + 512 r): the per-thread rows give bits 9..11, the thread index bits
+// 0..8, and the chunk totals (summed in warp 0 while the next chunk loads)
+// the bits above 11, in FP32 pairs on the lanes of warp 0.
+// ---------------------------------------------------------------------------
+constexpr int kMbThreads = 512;
+constexpr int kMbRows = 8;  // 4096 / 512
+constexpr int kMbStages = 3;
+constexpr int kMbChunkBits = 12;
+constexpr int kMbWarps = kMbThreads / 32;
+constexpr uint32_t kMbDrainLimit = 1u << 22;
+static_assert(kMbThreads * kMbRows == (1 << kMbChunkBits), "a chunk is one amplitude per thread and row");
+static_assert(kMbChunkBits == kF2ChunkBits, "both passes use the same chunks");
+
+template <int SRC>
+struct MbAmp {
+  using T = double2;
+};
+template <>
+struct MbAmp<1> {
+  using T = float2;
+};
+template <int SRC>
+constexpr size_t mass_bulk_smem() {
+  return (size_t)kMbStages * ((size_t)1 << kMbChunkBits) * sizeof(typename MbAmp<SRC>::T);
+}
+static_assert(mass_bulk_smem<0>() >= 4 * kMbThreads * sizeof(double), "the final fold reuses the ring");
+
+// x -> (hi, lo) for a probability: hi = x truncated to 24 significant bits,
+// lo = the remaining 29 bits rounded to 23 (x keeps 47 bits: relative error
+// <= 2^-47, unbiased). Integer operations and one FP32 subtraction: with
+// P = sign(x) 2^(e-23), e = x's exponent, lo = float(bits(P) + m) - P, m the
+// rounded remainder (a carry of m into P's exponent field is exact as well).
+// |x| outside [2^-103, 2^128) gives (0, 0): such squares are below 2^-206.
+__device__ __forceinline__ void split47(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int top = (unsigned int)(b >> 32), low = (unsigned int)b;
+  // (top << 3) | (low >> 29): the low 9 exponent bits, then 23 mantissa bits.
+  const unsigned int f = __funnelshift_r(low, top, 29);
+  // + 0x40000000 = - (896 << 23) mod 2^32: bits 30..23 become e + 127.
+  const unsigned int hb = ((f + 0x40000000u) & 0x7FFFFFFFu) | (top & 0x80000000u);
+  const unsigned int pb = (hb & 0xFF800000u) - (23u << 23);
+  const unsigned int m = ((low & 0x1FFFFFFFu) + 32u) >> 6;
+  const bool ok = (top & 0x7FFFFFFFu) - (920u << 20) < (231u << 20);  // exponent field in [920, 1150]
+  hi = ok ? __uint_as_float(hb) : 0.f;
+  lo = ok ? __fsub_rn(__uint_as_float(pb + m), __uint_as_float(pb)) : 0.f;
+}
+
+// x^2 as hi^2 (rounded) + its error: the exact FMA residual plus
+// lo (2 hi + lo). Relative error of the pair about 2^-46.
+__device__ __forceinline__ void sq_pair(float h, float l, float& p, float& e) {
+  p = __fmul_rn(h, h);
+  e = __fmaf_rn(h, h, -p);
+  e = __fmaf_rn(l, __fmaf_rn(h, 2.f, l), e);
+}
+
+template <int SRC>
+__device__ __forceinline__ F2 mb_prob(const typename MbAmp<SRC>::T a) {
+  float px, ex, py, ey;
+  if constexpr (SRC == 0) {
+    float xh, xl, yh, yl;
+    split47(a.x, xh, xl);
+    split47(a.y, yh, yl);
+    sq_pair(xh, xl, px, ex);
+    sq_pair(yh, yl, py, ey);
+  } else {
+    sq_pair(a.x, 0.f, px, ex);
+    sq_pair(a.y, 0.f, py, ey);
+  }
+  const float t = __fadd_rn(px, py);  // TwoSum(px, py) = t + q exactly
+  const float z = __fsub_rn(t, px);
+  const float q = __fadd_rn(__fsub_rn(px, __fsub_rn(t, z)), __fsub_rn(py, z));
+  return F2{t, __fadd_rn(q, __fadd_rn(ex, ey))};
+}
+
+// Thread 0: starts the bulk copy of the CTA's i-th chunk (global chunk
+// blockIdx.x + i * gridDim.x) into ring buffer i % kMbStages.
+template <typename A>
+__device__ __forceinline__ void mb_issue(A* ring, uint64_t* full, const A* gsrc, int64_t i) {
+  constexpr int C = 1 << kMbChunkBits;
+  constexpr uint32_t kBytes = (uint32_t)(C * sizeof(A));
+  const int s = (int)(i % kMbStages);
+  mbar_arrive_expect_tx(&full[s], kBytes);
+  bulk_load(ring + (size_t)s * C, gsrc + ((blockIdx.x + i * (int64_t)gridDim.x) << kMbChunkBits), kBytes,
+            &full[s]);
+}
+
+// After a wait for chunk i that gave up: thread 0 sets *status and waits
+// (bounded) for the copies still in flight (chunks i .. i + 2) before the
+// CTA returns.
+__device__ __forceinline__ void mb_give_up(uint64_t* full, int64_t i, int64_t count, int* status) {
+  if (threadIdx.x == 0) {
+    atomicExch(status, 1);
+    for (int64_t j = i; j < count && j < i + kMbStages; ++j)
+      mbar_wait(&full[j % kMbStages], (uint32_t)((j / kMbStages) & 1), kMbDrainLimit);
+  }
+}
+
+// Barrier init and the first kMbStages copies.
+template <typename A>
+__device__ __forceinline__ void mb_start(A* ring, uint64_t* full, const A* gsrc, int64_t count) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kMbStages; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int64_t i = 0; i < kMbStages && i < count; ++i) mb_issue(ring, full, gsrc, i);
+}
+
+// Warp 0: the block total of one chunk from the 16 warp sums in `red`; lane 0
+// writes the chunk's mass, lane j adds it to bit (12 + j)'s accumulator.
+__device__ __forceinline__ void mb_fold_chunk(const F2* red, int64_t ch, int nh, int lane, double* chunk_mass,
+                                              F2& hacc) {
+  F2 t = lane < kMbWarps ? red[lane] : F2{0.f, 0.f};
+#pragma unroll
+  for (int o = kMbWarps / 2; o > 0; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, t.h, o);
+    const float l = __shfl_xor_sync(0xffffffffu, t.l, o);
+    f2_add(t, h, l);
+  }
+  t.h = __shfl_sync(0xffffffffu, t.h, 0);
+  t.l = __shfl_sync(0xffffffffu, t.l, 0);
+  if (lane == 0) chunk_mass[ch] = f2_val(t);
+  if (lane < nh && ((ch >> lane) & 1)) f2_add(hacc, t.h, t.l);
+}
+
+// Outputs as k_chunk_mass_f2 with chunk_bits = 12: chunk_mass[ch], and per CTA
+// the n + 1 sums in `partial`. The grid is at most num_chunks; CTA b takes
+// chunks b, b + grid, ... A bulk-copy wait that gives up after `wait_limit`
+// polls sets *status to 1, waits for the CTA's copies in flight and returns.
+template <int SRC>
+__global__ void __launch_bounds__(kMbThreads, 1)
+k_chunk_mass_bulk(const void* src, int n, int64_t num_chunks, double* __restrict__ chunk_mass,
+                  double* __restrict__ partial, uint32_t wait_limit, int* __restrict__ status) {
+  using A = typename MbAmp<SRC>::T;
+  constexpr int C = 1 << kMbChunkBits;
+  extern __shared__ __align__(128) unsigned char mb_smem[];
+  A* ring = reinterpret_cast<A*>(mb_smem);
+  __shared__ __align__(8) uint64_t full[kMbStages];
+  __shared__ F2 red[2][kMbWarps];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nh = n - kMbChunkBits;  // <= 22 (34 qubits): one lane of warp 0 per bit
+  const int64_t G = gridDim.x;
+  const int64_t count = (num_chunks - blockIdx.x + G - 1) / G;
+  const A* gsrc = static_cast<const A*>(src);
+  mb_start(ring, full, gsrc, count);
+  F2 v[kMbRows];
+#pragma unroll
+  for (int r = 0; r < kMbRows; ++r) v[r] = F2{0.f, 0.f};
+  F2 hacc{0.f, 0.f};
+  for (int64_t i = 0; i < count; ++i) {
+    const int s = (int)(i % kMbStages);
+    const bool ok = mbar_wait(&full[s], (uint32_t)((i / kMbStages) & 1), wait_limit);
+    A a[kMbRows];
+#pragma unroll
+    for (int r = 0; r < kMbRows; ++r) a[r] = ring[(size_t)s * C + tid + kMbThreads * r];
+    // All reads of buffer s are done (its refill may start) and the previous
+    // chunk's warp sums are in `red`.
+    if (__syncthreads_or(!ok)) {
+      mb_give_up(full, i, count, status);
+      return;
+    }
+    if (tid == 0 && i + kMbStages < count) mb_issue(ring, full, gsrc, i + kMbStages);
+    if (warp == 0 && i > 0) mb_fold_chunk(red[(i - 1) & 1], blockIdx.x + (i - 1) * G, nh, lane, chunk_mass, hacc);
+    F2 p[kMbRows];
+#pragma unroll
+    for (int r = 0; r < kMbRows; ++r) {
+      p[r] = mb_prob<SRC>(a[r]);
+      f2_add(v[r], p[r].h, p[r].l);
+    }
+#pragma unroll
+    for (int w = 1; w < kMbRows; w <<= 1)
+#pragma unroll
+      for (int r = 0; r < kMbRows; r += 2 * w) f2_add(p[r], p[r + w].h, p[r + w].l);
+    const F2 mine = f2_warp_sum(p[0]);
+    if (lane == 0) red[i & 1][warp] = mine;
+  }
+  __syncthreads();  // the last warp sums are in `red`; every copy has landed
+  if (warp == 0) mb_fold_chunk(red[(count - 1) & 1], blockIdx.x + (count - 1) * G, nh, lane, chunk_mass, hacc);
+  // Fold the rows in FP32 pairs; FP64 for the per-thread results, in the ring.
+  F2 T{0.f, 0.f};
+  F2 R[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+  for (int r = 0; r < kMbRows; ++r) {
+    f2_add(T, v[r].h, v[r].l);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if ((r >> j) & 1) f2_add(R[j], v[r].h, v[r].l);
+  }
+  double* tsum = reinterpret_cast<double*>(mb_smem);
+  double* rsum = tsum + kMbThreads;  // [3][kMbThreads]
+  tsum[tid] = f2_val(T);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) rsum[j * kMbThreads + tid] = f2_val(R[j]);
+  __syncthreads();
+  double* out = partial + (int64_t)blockIdx.x * (n + 1);
+  if (tid < kMbChunkBits) {
+    double acc = 0.;
+    if (tid < 9) {
+      for (int t = 0; t < kMbThreads; ++t)
+        if ((t >> tid) & 1) acc += tsum[t];
+    } else {
+      for (int t = 0; t < kMbThreads; ++t) acc += rsum[(tid - 9) * kMbThreads + t];
+    }
+    out[tid] = acc;
+  } else if (tid == kMbThreads - 1) {
+    double acc = 0.;
+    for (int t = 0; t < kMbThreads; ++t) acc += tsum[t];
+    out[n] = acc;
+  }
+  if (warp == 0 && lane < nh) out[kMbChunkBits + lane] = f2_val(hacc);
+}
+
+// The sampler's segment prefixes for states of 12 or more qubits, staged as
+// in k_chunk_mass_bulk: 4096-amplitude chunks of 16 segments of 256; warp w
+// sums segment w (lane l: elements l + 32 r), warp 0 scans the 16 segment
+// masses of the previous chunk while the next one is summed. Outputs as
+// k_segment_prefix_f2 with seg_bits 8 and chunk_bits 12.
+constexpr int kSpSegBits = 8;
+static_assert((kMbChunkBits - kSpSegBits) == 4 && kMbWarps == 16, "one warp per segment");
+
+__device__ __forceinline__ void sp_fold_chunk(const F2* red, int64_t c, int lane, double* seg_incl,
+                                              double* chunk_mass) {
+  constexpr int spc = 1 << (kMbChunkBits - kSpSegBits);
+  F2 t = lane < spc ? red[lane] : F2{0.f, 0.f};
+#pragma unroll
+  for (int o = 1; o < spc; o <<= 1) {  // inclusive scan over lanes 0..15
+    const float h = __shfl_up_sync(0xffffffffu, t.h, o);
+    const float l = __shfl_up_sync(0xffffffffu, t.l, o);
+    if (lane >= o) {
+      F2 u{h, l};
+      f2_add(u, t.h, t.l);
+      t = u;
+    }
+  }
+  if (lane < spc) seg_incl[c * spc + lane] = f2_val(t);
+  if (lane == spc - 1) chunk_mass[c] = f2_val(t);
+}
+
+template <int SRC>
+__global__ void __launch_bounds__(kMbThreads, 1)
+k_segment_prefix_bulk(const void* src, int64_t num_chunks, double* __restrict__ seg_incl,
+                      double* __restrict__ chunk_mass, uint32_t wait_limit, int* __restrict__ status) {
+  using A = typename MbAmp<SRC>::T;
+  constexpr int C = 1 << kMbChunkBits;
+  extern __shared__ __align__(128) unsigned char mb_smem[];
+  A* ring = reinterpret_cast<A*>(mb_smem);
+  __shared__ __align__(8) uint64_t full[kMbStages];
+  __shared__ F2 red[2][kMbWarps];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t G = gridDim.x;
+  const int64_t count = (num_chunks - blockIdx.x + G - 1) / G;
+  const A* gsrc = static_cast<const A*>(src);
+  mb_start(ring, full, gsrc, count);
+  for (int64_t i = 0; i < count; ++i) {
+    const int s = (int)(i % kMbStages);
+    const bool ok = mbar_wait(&full[s], (uint32_t)((i / kMbStages) & 1), wait_limit);
+    A a[kMbRows];
+#pragma unroll
+    for (int r = 0; r < kMbRows; ++r) a[r] = ring[(size_t)s * C + (warp << kSpSegBits) + lane + 32 * r];
+    if (__syncthreads_or(!ok)) {
+      mb_give_up(full, i, count, status);
+      return;
+    }
+    if (tid == 0 && i + kMbStages < count) mb_issue(ring, full, gsrc, i + kMbStages);
+    if (warp == 0 && i > 0) sp_fold_chunk(red[(i - 1) & 1], blockIdx.x + (i - 1) * G, lane, seg_incl, chunk_mass);
+    F2 acc = mb_prob<SRC>(a[0]);
+#pragma unroll
+    for (int r = 1; r < kMbRows; ++r) {
+      const F2 p = mb_prob<SRC>(a[r]);
+      f2_add(acc, p.h, p.l);
+    }
+    acc = f2_warp_sum(acc);
+    if (lane == 0) red[i & 1][warp] = acc;
+  }
+  __syncthreads();
+  if (warp == 0) sp_fold_chunk(red[(count - 1) & 1], blockIdx.x + (count - 1) * G, lane, seg_incl, chunk_mass);
+}
 
 // Sum the per-CTA partials in CTA order.
 __global__ void k_reduce_partials(const double* __restrict__ partial, int width, int rows,
@@ -671,18 +963,58 @@ k_adjoint_step(typename P::G* __restrict__ psi, typename P::G* __restrict__ lam,
 }
 
 int chunk_bits_for(int n) { return std::min(kMaxChunkBits, n); }
-// Chunks of the Pauli-Z mass pass (k_chunk_mass_f2): 4096 amplitudes.
+// Chunks of the Pauli-Z mass pass (k_chunk_mass_bulk, k_chunk_mass_f2 below
+// 12 qubits): 4096 amplitudes.
 int mass_chunk_bits_for(int n) { return std::min(kF2ChunkBits, n); }
-// Its grid: eight CTAs per SM (two CTAs per SM measured 1.4x slower: too few
-// loads in flight).
-int mass_grid_for_chunks(int64_t num_chunks) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>(num_chunks, (int64_t)sm_count() * 8));
+
+// Amplitude states of 12 or more qubits take the bulk-staged pass.
+bool mass_uses_bulk(int src_kind, int n) { return src_kind != 2 && n >= kMbChunkBits; }
+
+// Its grid: one CTA per SM for the bulk-staged pass; eight CTAs per SM for
+// k_chunk_mass_f2 (two measured 1.4x slower: too few loads in flight).
+int mass_grid_for(int src_kind, int n, int64_t num_chunks) {
+  const int64_t per_sm = mass_uses_bulk(src_kind, n) ? 1 : 8;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(num_chunks, (int64_t)sm_count() * per_sm));
+}
+
+// Opts the bulk-staged pass into its shared memory (once per process; done
+// before any graph capture by the batch engine's setup).
+template <int SRC>
+void mass_bulk_attributes() {
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      k_chunk_mass_bulk<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mass_bulk_smem<SRC>());
+  (void)attr;  // a refusal shows as the launch's error
+}
+
+template <int SRC>
+void launch_mass_bulk(const void* src, int n, int64_t num_chunks, int grid, double* mass, double* partial,
+                      cudaStream_t stream) {
+  constexpr size_t smem = mass_bulk_smem<SRC>();
+  mass_bulk_attributes<SRC>();
+  k_chunk_mass_bulk<SRC><<<grid, kMbThreads, smem, stream>>>(src, n, num_chunks, mass, partial, tma_wait_limit(),
+                                                             tma_status_word());
+}
+
+template <int SRC>
+void launch_prefix_bulk(const void* src, int64_t num_chunks, int grid, double* seg, double* mass,
+                        cudaStream_t stream) {
+  constexpr size_t smem = mass_bulk_smem<SRC>();
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_segment_prefix_bulk<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  (void)attr;  // a refusal shows as the launch's error
+  k_segment_prefix_bulk<SRC><<<grid, kMbThreads, smem, stream>>>(src, num_chunks, seg, mass, tma_wait_limit(),
+                                                                 tma_status_word());
 }
 
 // The per-chunk / per-bit mass pass: FP32 pairs for amplitudes (src_kind 0
 // complex128, 1 complex64), FP64 for a probability vector (src_kind 2).
 void launch_mass_kernel(const void* src, int src_kind, int n, int cb, int64_t num_chunks, int grid, double* mass,
                         double* partial, cudaStream_t stream) {
+  if (mass_uses_bulk(src_kind, n)) {
+    if (src_kind == 0) launch_mass_bulk<0>(src, n, num_chunks, grid, mass, partial, stream);
+    else launch_mass_bulk<1>(src, n, num_chunks, grid, mass, partial, stream);
+    return;
+  }
   switch (src_kind) {
     case 0: k_chunk_mass_f2<0><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
     case 1: k_chunk_mass_f2<1><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
@@ -701,7 +1033,7 @@ int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& chunk_de
                     int64_t* num_chunks_out, int* chunk_bits_out) {
   const int cb = src_kind == 2 ? chunk_bits_for(n) : mass_chunk_bits_for(n);
   const int64_t num_chunks = int64_t(1) << (n - cb);
-  const int grid = src_kind == 2 ? grid_for_chunks(num_chunks) : mass_grid_for_chunks(num_chunks);
+  const int grid = src_kind == 2 ? grid_for_chunks(num_chunks) : mass_grid_for(src_kind, n, num_chunks);
   DMV_TRY(chunk_dev.reserve((size_t)num_chunks * sizeof(double)));
   const size_t partial_elems = (size_t)grid * (n + 1);
   DMV_TRY(reduce_dev.reserve((partial_elems + (size_t)(n + 1)) * sizeof(double)));
@@ -731,8 +1063,9 @@ struct SamplePrefix {
 int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefix, cudaStream_t stream,
                        SamplePrefix* out) {
   SamplePrefix sp;
-  sp.seg_bits = std::min(8, n);
-  sp.chunk_bits = chunk_bits_for(n);
+  const bool bulk = mass_uses_bulk(src_kind, n);
+  sp.seg_bits = std::min(kSpSegBits, n);
+  sp.chunk_bits = bulk ? kMbChunkBits : chunk_bits_for(n);
   sp.num_chunks = int64_t(1) << (n - sp.chunk_bits);
   const int64_t nseg = int64_t(1) << (n - sp.seg_bits);
   DMV_TRY(prefix.reserve((size_t)(2 * sp.num_chunks + nseg) * sizeof(double) +
@@ -741,11 +1074,17 @@ int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefi
   double* incl = mass + sp.num_chunks;
   double* seg = incl + sp.num_chunks;
   int32_t* guide = reinterpret_cast<int32_t*>(seg + nseg);
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 7) / 8, (int64_t)sm_count() * 8));
-  switch (src_kind) {
-    case 0: k_segment_prefix_f2<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
-    case 1: k_segment_prefix_f2<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
-    default: k_segment_prefix<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+  if (bulk) {
+    const int grid = mass_grid_for(src_kind, n, sp.num_chunks);
+    if (src_kind == 0) launch_prefix_bulk<0>(src, sp.num_chunks, grid, seg, mass, stream);
+    else launch_prefix_bulk<1>(src, sp.num_chunks, grid, seg, mass, stream);
+  } else {
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 7) / 8, (int64_t)sm_count() * 8));
+    switch (src_kind) {
+      case 0: k_segment_prefix_f2<0><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+      case 1: k_segment_prefix_f2<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+      default: k_segment_prefix<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
+    }
   }
   k_scan_chunks<<<1, 1024, 0, stream>>>(mass, sp.num_chunks, incl);
   const int gg = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 256) / 256, (int64_t)sm_count() * 4));
@@ -784,6 +1123,7 @@ int run_sampler(const void* src, int src_kind, int n, DeviceBuffer& prefix, Devi
   DMV_TRY(launch_warp_sampler(src, src_kind, sp, u_dev, k, out_dev, stream));
   DMV_CUDA_TRY(cudaMemcpyAsync(samples_host, out_dev, (size_t)k * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
   DMV_CUDA_TRY(cudaStreamSynchronize(stream));
+  DMV_TRY(check_window_status());  // the prefix pass's chunk load waits
   return DMV_OK;
 }
 
@@ -793,7 +1133,9 @@ ChunkMassShape chunk_mass_shape(int n) {
   ChunkMassShape sh;
   sh.chunk_bits = mass_chunk_bits_for(n);
   sh.num_chunks = int64_t(1) << (n - sh.chunk_bits);
-  sh.grid = mass_grid_for_chunks(sh.num_chunks);
+  sh.grid = mass_grid_for(0, n, sh.num_chunks);  // the same grid for complex64
+  mass_bulk_attributes<0>();
+  mass_bulk_attributes<1>();
   sh.partial_elems = (int64_t)sh.grid * (n + 1);
   return sh;
 }
@@ -830,6 +1172,7 @@ int launch_expect_z(dmv_state_s* s, double* expect_host, double* norm_host) {
   std::vector<double> h((size_t)s->n + 1);
   DMV_CUDA_TRY(cudaMemcpyAsync(h.data(), sums, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  DMV_TRY(check_window_status());  // the mass pass's chunk load waits
   const double total = h[(size_t)s->n];
   if (expect_host)
     for (int q = 0; q < s->n; ++q) expect_host[q] = total - 2.0 * h[(size_t)q];
@@ -879,6 +1222,7 @@ int launch_sample_counts(dmv_state_s* s, const double* uniforms_host, uint64_t s
   DMV_CUDA_TRY(cudaMemcpyAsync(counts_host, counts_dev, 64 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                s->stream));
   DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  DMV_TRY(check_window_status());  // the prefix pass's chunk load waits
   return DMV_OK;
 }
 

@@ -113,6 +113,86 @@ def test_expectation_and_norm_on_random_states(built_lib, oracle_mod):
             free_state(st)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_mass_pass_chunk_and_grid_edges(built_lib, oracle_mod, precision):
+    """<Z_q> and the norm around the mass pass's chunk (4096 amplitudes) and grid
+    (one CTA per SM, fewer or uneven chunks per CTA) edges, on states with exact
+    zeros, amplitudes below the 2^-103 flush level and norms far from 1."""
+    from damavand_gb300._lib import check, dptr, lib
+    rng = np.random.default_rng(7)
+    for n, scale in ((11, 1.0), (12, 1.0), (13, 2.0 ** 40), (20, 1.0), (22, 2.0 ** -30)):
+        psi = random_state(n, rng) * scale
+        psi[rng.integers(0, 1 << n, 64)] = 0
+        psi[rng.integers(0, 1 << n, 64)] = 2.0 ** -110 * scale * (1 - 1j)
+        if precision == 1:
+            psi = psi.astype(np.complex64).astype(np.complex128)
+        st = new_state(n, precision)
+        try:
+            load_state(st, psi)
+            ez = np.empty(n)
+            nrm = np.empty(1)
+            check(lib.dmv_expect_z(st.handle, dptr(ez), dptr(nrm)))
+            p = oracle_mod.measure(psi)
+            s2 = scale * scale
+            assert np.max(np.abs(ez - oracle_mod.expect_z(p))) <= EXPECT_ATOL * s2, (n, precision)
+            assert abs(nrm[0] - p.sum()) <= 1e-13 * s2, (n, precision)
+        finally:
+            free_state(st)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_state_sampling_chunk_and_grid_edges(built_lib, oracle_mod, precision):
+    """Inverse-CDF samples of loaded states around the prefix pass's chunk (4096
+    amplitudes, 16 segments of 256) and grid edges, with an empty segment, an
+    empty chunk and single zero amplitudes, against the oracle's sampler."""
+    from damavand_gb300._lib import check, dptr, lib, u64ptr
+    rng = np.random.default_rng(9)
+    for n in (11, 12, 13, 20):
+        psi = random_state(n, rng)
+        psi[rng.integers(0, 1 << n, 200)] = 0
+        psi[256:512] = 0  # a whole segment
+        if n > 12:
+            psi[1 << 12: 2 << 12] = 0  # a whole chunk
+        psi /= np.linalg.norm(psi)
+        if precision == 1:
+            psi = psi.astype(np.complex64).astype(np.complex128)
+        st = new_state(n, precision)
+        try:
+            load_state(st, psi)
+            u = np.concatenate([[0.0, 0.5, 1.0 - 2.0 ** -53], rng.random(3000)])
+            out = np.empty(u.size, dtype=np.uint64)
+            check(lib.dmv_sample(st.handle, dptr(u), u.size, u64ptr(out)))
+            p = oracle_mod.measure(psi)
+            assert assert_samples_match(p, u, out, oracle_mod) <= 2, n
+            assert np.all(p[out[1:]] > 0)
+        finally:
+            free_state(st)
+
+
+def test_mass_pass_wait_limit_reports_timeout(built_lib, oracle_mod):
+    """A chunk-load wait of the mass pass that gives up (limit 0 polls) drains the
+    CTA's copies, returns, and surfaces as DMV_ERR_TIMEOUT from the same call;
+    with the default limit the same state then reads out correctly."""
+    from damavand_gb300._lib import ERR_TIMEOUT, check, dptr, lib
+    n = 16
+    psi = random_state(n, np.random.default_rng(8))
+    st = new_state(n)
+    try:
+        load_state(st, psi)
+        ez = np.empty(n)
+        check(lib.dmv_debug_tma_wait_limit(0))
+        try:
+            rc = lib.dmv_expect_z(st.handle, dptr(ez), None)
+        finally:
+            check(lib.dmv_debug_tma_wait_limit(-1))
+        assert rc == ERR_TIMEOUT
+        check(lib.dmv_state_synchronize(st.handle))  # flag cleared
+        check(lib.dmv_expect_z(st.handle, dptr(ez), None))
+        assert np.max(np.abs(ez - oracle_mod.expect_z(oracle_mod.measure(psi)))) <= EXPECT_ATOL
+    finally:
+        free_state(st)
+
+
 def test_fidelity_on_device(built_lib, oracle_mod):
     from damavand_gb300 import Circuit
     from damavand_gb300.workloads import add_to_circuit, parameters, ring_ansatz
