@@ -153,7 +153,7 @@ struct dmv_batch_s {
   void* arena = nullptr;
   cudaStream_t stream = nullptr;
   DeviceBuffer passes_dev, items_dev, ops_dev, counters_dev, offsets_dev, reduce_dev;
-  std::vector<int64_t> red_mass, red_partial, red_sums;  // per-circuit offsets (doubles) into reduce_dev
+  std::vector<int64_t> red_partial, red_sums;  // per-circuit offsets (doubles) into reduce_dev
   int64_t num_items = 0, num_passes = 0, num_ops = 0;
   int32_t max_k = 0;
   PlanOptions opt;
@@ -318,7 +318,7 @@ int batch_enqueue(dmv_batch_s* b) {
   double* red = static_cast<double*>(b->reduce_dev.ptr);
   for (int32_t c = 0; c < b->count; ++c) {
     const char* base = static_cast<const char*>(b->arena) + (size_t)b->offsets[(size_t)c] * b->amp_size();
-    DMV_TRY(launch_chunk_mass_into(base, b->precision == DMV_C128 ? 0 : 1, b->n[(size_t)c], red + b->red_mass[(size_t)c],
+    DMV_TRY(launch_chunk_mass_into(base, b->precision == DMV_C128 ? 0 : 1, b->n[(size_t)c],
                                    red + b->red_partial[(size_t)c], red + b->red_sums[(size_t)c], b->stream));
   }
   return DMV_OK;
@@ -438,8 +438,6 @@ extern "C" int dmv_batch_create(int32_t num_circuits, const int32_t* num_qubits,
     int64_t red = 0;
     for (int32_t c = 0; c < num_circuits; ++c) {
       const ChunkMassShape sh = chunk_mass_shape(b->n[(size_t)c]);
-      b->red_mass.push_back(red);
-      red += sh.num_chunks;
       b->red_partial.push_back(red);
       red += sh.partial_elems;
       b->red_sums.push_back(red);

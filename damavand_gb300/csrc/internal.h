@@ -368,9 +368,9 @@ uint32_t tma_wait_limit();
 // The device word those waits set to 1 when they give up.
 int* tma_status_word();
 
-// Chunk-mass / Pauli-Z reduction into caller-provided device buffers:
-// `mass` holds num_chunks doubles, `partial` partial_elems, `sums` n+1
-// (mass with bit q set for q < n, then the total).
+// Pauli-Z mass reduction into caller-provided device buffers: `partial`
+// holds partial_elems doubles, `sums` n+1 (mass with bit q set for q < n,
+// then the total).
 struct ChunkMassShape {
   int chunk_bits;
   int64_t num_chunks;
@@ -378,6 +378,6 @@ struct ChunkMassShape {
   int64_t partial_elems;
 };
 ChunkMassShape chunk_mass_shape(int n);
-int launch_chunk_mass_into(const void* src, int src_kind, int n, double* mass, double* partial, double* sums,
+int launch_chunk_mass_into(const void* src, int src_kind, int n, double* partial, double* sums,
                            cudaStream_t stream);
 }  // namespace dmv

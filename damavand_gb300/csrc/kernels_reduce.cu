@@ -22,7 +22,6 @@ namespace {
 
 constexpr int kRedThreads = 256;
 constexpr int kMaxChunkBits = 13;  // 8192 amplitudes per chunk
-constexpr int kRowsPerThread = 32; // (1 << kMaxChunkBits) / kRedThreads
 
 int sm_count() {
   static int sms = 0;
@@ -77,85 +76,13 @@ k_probabilities(const void* src, double* __restrict__ out, int64_t N) {
     out[i] = prob_at<SRC>(src, i);
 }
 
-// Per-chunk probability mass and per-qubit "bit set" mass.
-// Element e of a chunk is e = tid + 256*r. Each thread keeps one accumulator
-// per r across all chunks it visits, so the inner loop costs one FP64 add per
-// element; the bit sums are formed once per CTA at the end.
-// partial[cta * (n+1) + q] = sum of p over indices with bit q set, q < n;
-// partial[cta * (n+1) + n] = sum of all p.
-template <int SRC>
-__global__ void __launch_bounds__(kRedThreads)
-k_chunk_mass(const void* src, int n, int chunk_bits, int64_t num_chunks,
-             double* __restrict__ chunk_mass, double* __restrict__ partial) {
-  __shared__ double red[32];
-  __shared__ double tsum[kRedThreads];
-  __shared__ double rsum[5][kRedThreads];
-  const int C = 1 << chunk_bits;
-  double v[kRowsPerThread];
-#pragma unroll
-  for (int r = 0; r < kRowsPerThread; ++r) v[r] = 0.;
-  __shared__ double hi_acc[34];  // only thread 0 updates it
-  if (threadIdx.x < 34) hi_acc[threadIdx.x] = 0.;
-
-  for (int64_t ch = blockIdx.x; ch < num_chunks; ch += gridDim.x) {
-    const int64_t base = ch << chunk_bits;
-    double mine = 0.;
-#pragma unroll
-    for (int r = 0; r < kRowsPerThread; ++r) {
-      const int e = threadIdx.x + kRedThreads * r;
-      if (e < C) {
-        const double p = prob_at<SRC>(src, base + e);
-        v[r] += p;
-        mine += p;
-      }
-    }
-    const double tot = block_sum(mine, red);
-    if (threadIdx.x == 0) {
-      chunk_mass[ch] = tot;
-      for (int j = 0; j < n - chunk_bits; ++j)
-        if ((ch >> j) & 1) hi_acc[j] += tot;
-    }
-  }
-  // Fold per-thread accumulators into bit sums.
-  double T = 0.;
-  double R[5] = {0., 0., 0., 0., 0.};
-#pragma unroll
-  for (int r = 0; r < kRowsPerThread; ++r) {
-    T += v[r];
-#pragma unroll
-    for (int j = 0; j < 5; ++j)
-      if ((r >> j) & 1) R[j] += v[r];
-  }
-  tsum[threadIdx.x] = T;
-#pragma unroll
-  for (int j = 0; j < 5; ++j) rsum[j][threadIdx.x] = R[j];
-  __syncthreads();
-  double* out = partial + (int64_t)blockIdx.x * (n + 1);
-  const int q = threadIdx.x;
-  if (q < chunk_bits) {
-    double acc = 0.;
-    if (q < 8) {
-      for (int t = 0; t < kRedThreads; ++t)
-        if ((t >> q) & 1) acc += tsum[t];
-    } else {
-      for (int t = 0; t < kRedThreads; ++t) acc += rsum[q - 8][t];
-    }
-    out[q] = acc;
-  } else if (q == 64) {
-    double acc = 0.;
-    for (int t = 0; t < kRedThreads; ++t) acc += tsum[t];
-    out[n] = acc;
-  }
-  if (threadIdx.x == 0) {
-    for (int j = 0; j < n - chunk_bits; ++j) out[chunk_bits + j] = hi_acc[j];
-  }
-}
-
 // ---------------------------------------------------------------------------
-// The same per-chunk and per-bit masses in FP32 pairs (k_chunk_mass_f2).
+// Pauli-Z masses: per qubit q the probability mass of the indices with bit q
+// set, and the total (<Z_q> = total - 2 mass_q), in FP32 pairs.
 //
-// On GB300 the FP64 reduction above spends 4 FP64 operations per amplitude
-// and runs at about a third of HBM speed. Here every probability is formed
+// On GB300 an FP64 reduction spends 4 FP64 operations per amplitude and runs
+// at about a third of HBM speed (8.8 ms at 30 qubits against 2.5 ms for the
+// read). Here every probability is formed
 // and summed as an unevaluated pair of floats hi + lo: the components of a
 // complex128 amplitude are split into FP32 pairs with integer operations
 // (split_f64), x^2 is hi^2 exactly by FMA (TwoProd) plus the cross terms,
@@ -220,13 +147,16 @@ __device__ __forceinline__ F2 f2_warp_sum(F2 v) {
 constexpr int kF2Rows = 16;  // chunk of kRedThreads x 16 = 4096 amplitudes
 constexpr int kF2ChunkBits = 12;
 
-// As k_chunk_mass (same outputs: chunk_mass[ch], and per CTA the n + 1 sums
-// `partial`), in FP32 pairs, for complex128 (SRC 0) and complex64 (SRC 1)
-// amplitudes, with 4096-amplitude chunks (chunk_bits = min(n, 12)).
+// Register-fed mass pass (states below 12 qubits; k_chunk_mass_bulk above),
+// for complex128 (SRC 0) and complex64 (SRC 1) amplitudes, with
+// 2^chunk_bits-amplitude chunks (chunk_bits = min(n, 12)). Element e of a
+// chunk is e = tid + 256 r; each thread keeps one accumulator per r across
+// the chunks it visits, and thread 0 adds each chunk's total to the masses of
+// the chunk-index bits. Per CTA: partial[cta * (n+1) + q] = mass with bit q
+// set (q < n), partial[cta * (n+1) + n] = the total.
 template <int SRC>
 __global__ void __launch_bounds__(kRedThreads)
-k_chunk_mass_f2(const void* src, int n, int chunk_bits, int64_t num_chunks, double* __restrict__ chunk_mass,
-                double* __restrict__ partial) {
+k_chunk_mass_f2(const void* src, int n, int chunk_bits, int64_t num_chunks, double* __restrict__ partial) {
   __shared__ F2 red[kRedThreads / 32];
   __shared__ double tsum[kRedThreads];
   __shared__ double rsum[4][kRedThreads];
@@ -257,7 +187,6 @@ k_chunk_mass_f2(const void* src, int n, int chunk_bits, int64_t num_chunks, doub
       F2 tot{0.f, 0.f};
       for (int w = 0; w < kRedThreads / 32; ++w) f2_add(tot, red[w].h, red[w].l);
       const double t = f2_val(tot);
-      chunk_mass[ch] = t;
       for (int j = 0; j < n - chunk_bits; ++j)
         if ((ch >> j) & 1) hi_acc[j] += t;
     }
@@ -304,23 +233,27 @@ static_assert(kF2ChunkBits < kRedThreads - 1, "the total's thread is not a per-b
 //
 // The register-fed pass above keeps too few loads in flight per SM for HBM
 // speed (its grid sweep: two CTAs per SM ran at a quarter of HBM bandwidth,
-// eight at about half). Here one thread starts an untiled bulk copy
+// eight at about half). Here a producer warp starts one untiled bulk copy
 // (cp.async.bulk) per 4096-amplitude chunk into a ring of three buffers, so
-// two chunks (128 KB of complex128) are in flight while the third is summed,
-// whatever the register count. The arithmetic is cut to about 60 operations
-// per amplitude (split47 below, a TwoSum in place of a full pair addition for
-// |x|^2 + |y|^2). Each thread owns 8 amplitudes of a chunk (elements
-// tid + 512 r): the per-thread rows give bits 9..11, the thread index bits
-// 0..8, and the chunk totals (summed in warp 0 while the next chunk loads)
-// the bits above 11, in FP32 pairs on the lanes of warp 0.
+// up to three chunks (192 KB of complex128) are in flight whatever the
+// register count. Sixteen summing warps share no per-chunk barrier: each
+// releases a buffer on its "empty" mbarrier as soon as it has read its part,
+// and keeps everything else (row sums, its share of the high-bit masses) in
+// registers until the end, so a slow warp does not hold up the others. The
+// arithmetic is about 60 operations per amplitude (split47 below, a TwoSum in
+// place of a full pair addition for |x|^2 + |y|^2). Each summing thread owns 8
+// amplitudes of a chunk (elements tid + 512 r): the rows give bits 9..11, the
+// thread index bits 0..8, and each warp's chunk sum the bits above 11 (lane j
+// of every warp accumulates bit 12 + j).
 // ---------------------------------------------------------------------------
-constexpr int kMbThreads = 512;
-constexpr int kMbRows = 8;  // 4096 / 512
+constexpr int kMbSumWarps = 16;
+constexpr int kMbSumThreads = 32 * kMbSumWarps;  // 512
+constexpr int kMbThreads = kMbSumThreads + 32;   // + the producer warp
+constexpr int kMbRows = 8;                       // 4096 / 512
 constexpr int kMbStages = 3;
 constexpr int kMbChunkBits = 12;
-constexpr int kMbWarps = kMbThreads / 32;
 constexpr uint32_t kMbDrainLimit = 1u << 22;
-static_assert(kMbThreads * kMbRows == (1 << kMbChunkBits), "a chunk is one amplitude per thread and row");
+static_assert(kMbSumThreads * kMbRows == (1 << kMbChunkBits), "a chunk is one amplitude per thread and row");
 static_assert(kMbChunkBits == kF2ChunkBits, "both passes use the same chunks");
 
 template <int SRC>
@@ -335,7 +268,8 @@ template <int SRC>
 constexpr size_t mass_bulk_smem() {
   return (size_t)kMbStages * ((size_t)1 << kMbChunkBits) * sizeof(typename MbAmp<SRC>::T);
 }
-static_assert(mass_bulk_smem<0>() >= 4 * kMbThreads * sizeof(double), "the final fold reuses the ring");
+static_assert(mass_bulk_smem<1>() >= 4 * kMbSumThreads * sizeof(double) + kMbSumWarps * 32 * sizeof(double),
+              "the final fold reuses the ring");
 
 // x -> (hi, lo) for a probability: hi = x truncated to 24 significant bits,
 // lo = the remaining 29 bits rounded to 23 (x keeps 47 bits: relative error
@@ -384,209 +318,215 @@ __device__ __forceinline__ F2 mb_prob(const typename MbAmp<SRC>::T a) {
   return F2{t, __fadd_rn(q, __fadd_rn(ex, ey))};
 }
 
-// Thread 0: starts the bulk copy of the CTA's i-th chunk (global chunk
-// blockIdx.x + i * gridDim.x) into ring buffer i % kMbStages.
-template <typename A>
-__device__ __forceinline__ void mb_issue(A* ring, uint64_t* full, const A* gsrc, int64_t i) {
-  constexpr int C = 1 << kMbChunkBits;
-  constexpr uint32_t kBytes = (uint32_t)(C * sizeof(A));
-  const int s = (int)(i % kMbStages);
-  mbar_arrive_expect_tx(&full[s], kBytes);
-  bulk_load(ring + (size_t)s * C, gsrc + ((blockIdx.x + i * (int64_t)gridDim.x) << kMbChunkBits), kBytes,
-            &full[s]);
-}
+// The ring of a bulk-staged pass: full[s] completes when chunk i (i % 3 == s)
+// has landed (one arrival with its byte count), empty[s] when all summing
+// warps have read it (one arrival per warp). Every wait is bounded; a wait
+// that gives up sets *status to 1, and the party that gave up stops waiting
+// from then on (the producer stops issuing), so every thread still reaches
+// the closing barrier. The producer waits, bounded, for its last copies
+// before it gets there, so none is in flight when the CTA ends.
+struct BulkRing {
+  uint64_t full[kMbStages];
+  uint64_t empty[kMbStages];
+};
 
-// After a wait for chunk i that gave up: thread 0 sets *status and waits
-// (bounded) for the copies still in flight (chunks i .. i + 2) before the
-// CTA returns.
-__device__ __forceinline__ void mb_give_up(uint64_t* full, int64_t i, int64_t count, int* status) {
+__device__ __forceinline__ void ring_init(BulkRing& r) {
   if (threadIdx.x == 0) {
-    atomicExch(status, 1);
-    for (int64_t j = i; j < count && j < i + kMbStages; ++j)
-      mbar_wait(&full[j % kMbStages], (uint32_t)((j / kMbStages) & 1), kMbDrainLimit);
-  }
-}
-
-// Barrier init and the first kMbStages copies.
-template <typename A>
-__device__ __forceinline__ void mb_start(A* ring, uint64_t* full, const A* gsrc, int64_t count) {
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kMbStages; ++s) mbar_init(&full[s], 1);
+    for (int s = 0; s < kMbStages; ++s) {
+      mbar_init(&r.full[s], 1);
+      mbar_init(&r.empty[s], kMbSumWarps);
+    }
     fence_mbar_init();
   }
   __syncthreads();
-  if (threadIdx.x == 0)
-    for (int64_t i = 0; i < kMbStages && i < count; ++i) mb_issue(ring, full, gsrc, i);
 }
 
-// Warp 0: the block total of one chunk from the 16 warp sums in `red`; lane 0
-// writes the chunk's mass, lane j adds it to bit (12 + j)'s accumulator.
-__device__ __forceinline__ void mb_fold_chunk(const F2* red, int64_t ch, int nh, int lane, double* chunk_mass,
-                                              F2& hacc) {
-  F2 t = lane < kMbWarps ? red[lane] : F2{0.f, 0.f};
-#pragma unroll
-  for (int o = kMbWarps / 2; o > 0; o >>= 1) {
-    const float h = __shfl_xor_sync(0xffffffffu, t.h, o);
-    const float l = __shfl_xor_sync(0xffffffffu, t.l, o);
-    f2_add(t, h, l);
+// Producer warp, one lane: chunk i (global chunk blockIdx.x + i * gridDim.x)
+// into buffer i % 3 once the summing warps have released chunk i - 3.
+template <typename A>
+__device__ void ring_produce(BulkRing& r, A* ring, const A* gsrc, int64_t count, uint32_t wait_limit,
+                             int* status) {
+  constexpr int C = 1 << kMbChunkBits;
+  constexpr uint32_t kBytes = (uint32_t)(C * sizeof(A));
+  int64_t issued = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const int s = (int)(i % kMbStages);
+    if (i >= kMbStages && !mbar_wait(&r.empty[s], (uint32_t)((i / kMbStages - 1) & 1), wait_limit)) {
+      atomicExch(status, 1);
+      break;
+    }
+    mbar_arrive_expect_tx(&r.full[s], kBytes);
+    bulk_load(ring + (size_t)s * C, gsrc + ((blockIdx.x + i * (int64_t)gridDim.x) << kMbChunkBits), kBytes,
+              &r.full[s]);
+    issued = i + 1;
   }
-  t.h = __shfl_sync(0xffffffffu, t.h, 0);
-  t.l = __shfl_sync(0xffffffffu, t.l, 0);
-  if (lane == 0) chunk_mass[ch] = f2_val(t);
-  if (lane < nh && ((ch >> lane) & 1)) f2_add(hacc, t.h, t.l);
+  // Chunks before issued - 3 were released, so read, so landed.
+  for (int64_t j = issued > kMbStages ? issued - kMbStages : 0; j < issued; ++j)
+    mbar_wait(&r.full[j % kMbStages], (uint32_t)((j / kMbStages) & 1), kMbDrainLimit);
 }
 
-// Outputs as k_chunk_mass_f2 with chunk_bits = 12: chunk_mass[ch], and per CTA
-// the n + 1 sums in `partial`. The grid is at most num_chunks; CTA b takes
-// chunks b, b + grid, ... A bulk-copy wait that gives up after `wait_limit`
-// polls sets *status to 1, waits for the CTA's copies in flight and returns.
+// Summing warp: waits for chunk i; false (and *status set) if the wait gave up.
+__device__ __forceinline__ bool ring_wait_full(BulkRing& r, int64_t i, uint32_t wait_limit, int* status) {
+  const bool ok = __all_sync(0xffffffffu,
+                             mbar_wait(&r.full[i % kMbStages], (uint32_t)((i / kMbStages) & 1), wait_limit));
+  if (!ok && (threadIdx.x & 31) == 0) atomicExch(status, 1);
+  return ok;
+}
+
+// Summing warp: its reads of chunk i are done.
+__device__ __forceinline__ void ring_release(BulkRing& r, int64_t i) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(&r.empty[i % kMbStages]);
+}
+
+// Outputs as k_chunk_mass_f2 with chunk_bits = 12, except that no per-chunk
+// masses are written (nothing reads them): per CTA the n + 1 sums in
+// `partial`. The grid is at most num_chunks; CTA b takes chunks b, b + grid, ...
 template <int SRC>
 __global__ void __launch_bounds__(kMbThreads, 1)
-k_chunk_mass_bulk(const void* src, int n, int64_t num_chunks, double* __restrict__ chunk_mass,
-                  double* __restrict__ partial, uint32_t wait_limit, int* __restrict__ status) {
+k_chunk_mass_bulk(const void* src, int n, int64_t num_chunks, double* __restrict__ partial, uint32_t wait_limit,
+                  int* __restrict__ status) {
   using A = typename MbAmp<SRC>::T;
   constexpr int C = 1 << kMbChunkBits;
   extern __shared__ __align__(128) unsigned char mb_smem[];
   A* ring = reinterpret_cast<A*>(mb_smem);
-  __shared__ __align__(8) uint64_t full[kMbStages];
-  __shared__ F2 red[2][kMbWarps];
+  __shared__ __align__(8) BulkRing rb;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nh = n - kMbChunkBits;  // <= 22 (34 qubits): one lane of warp 0 per bit
+  const int nh = n - kMbChunkBits;  // <= 22 (34 qubits): one lane per bit
   const int64_t G = gridDim.x;
   const int64_t count = (num_chunks - blockIdx.x + G - 1) / G;
-  const A* gsrc = static_cast<const A*>(src);
-  mb_start(ring, full, gsrc, count);
+  ring_init(rb);
   F2 v[kMbRows];
 #pragma unroll
   for (int r = 0; r < kMbRows; ++r) v[r] = F2{0.f, 0.f};
   F2 hacc{0.f, 0.f};
-  for (int64_t i = 0; i < count; ++i) {
-    const int s = (int)(i % kMbStages);
-    const bool ok = mbar_wait(&full[s], (uint32_t)((i / kMbStages) & 1), wait_limit);
-    A a[kMbRows];
+  if (warp == kMbSumWarps) {
+    if (lane == 0) ring_produce(rb, ring, static_cast<const A*>(src), count, wait_limit, status);
+  } else {
+    for (int64_t i = 0; i < count; ++i) {
+      if (!ring_wait_full(rb, i, wait_limit, status)) break;
+      const A* buf = ring + (size_t)(i % kMbStages) * C;
+      A a[kMbRows];
 #pragma unroll
-    for (int r = 0; r < kMbRows; ++r) a[r] = ring[(size_t)s * C + tid + kMbThreads * r];
-    // All reads of buffer s are done (its refill may start) and the previous
-    // chunk's warp sums are in `red`.
-    if (__syncthreads_or(!ok)) {
-      mb_give_up(full, i, count, status);
-      return;
+      for (int r = 0; r < kMbRows; ++r) a[r] = buf[tid + kMbSumThreads * r];
+      ring_release(rb, i);
+      F2 p[kMbRows];
+#pragma unroll
+      for (int r = 0; r < kMbRows; ++r) {
+        p[r] = mb_prob<SRC>(a[r]);
+        f2_add(v[r], p[r].h, p[r].l);
+      }
+#pragma unroll
+      for (int w = 1; w < kMbRows; w <<= 1)
+#pragma unroll
+        for (int r = 0; r < kMbRows; r += 2 * w) f2_add(p[r], p[r + w].h, p[r + w].l);
+      F2 ws = f2_warp_sum(p[0]);
+      ws.h = __shfl_sync(0xffffffffu, ws.h, 0);  // every lane adds the same value
+      ws.l = __shfl_sync(0xffffffffu, ws.l, 0);
+      const int64_t ch = blockIdx.x + i * G;
+      if (lane < nh && ((ch >> lane) & 1)) f2_add(hacc, ws.h, ws.l);
     }
-    if (tid == 0 && i + kMbStages < count) mb_issue(ring, full, gsrc, i + kMbStages);
-    if (warp == 0 && i > 0) mb_fold_chunk(red[(i - 1) & 1], blockIdx.x + (i - 1) * G, nh, lane, chunk_mass, hacc);
-    F2 p[kMbRows];
+  }
+  __syncthreads();  // every copy has landed: the ring is free for the fold
+  // Rows folded in FP32 pairs; FP64 for the per-thread and per-warp results.
+  double* tsum = reinterpret_cast<double*>(mb_smem);
+  double* rsum = tsum + kMbSumThreads;         // [3][kMbSumThreads]
+  double* hsum = rsum + 3 * kMbSumThreads;     // [kMbSumWarps][32]
+  if (warp < kMbSumWarps) {
+    F2 T{0.f, 0.f};
+    F2 R[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
     for (int r = 0; r < kMbRows; ++r) {
-      p[r] = mb_prob<SRC>(a[r]);
-      f2_add(v[r], p[r].h, p[r].l);
+      f2_add(T, v[r].h, v[r].l);
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if ((r >> j) & 1) f2_add(R[j], v[r].h, v[r].l);
     }
+    tsum[tid] = f2_val(T);
 #pragma unroll
-    for (int w = 1; w < kMbRows; w <<= 1)
-#pragma unroll
-      for (int r = 0; r < kMbRows; r += 2 * w) f2_add(p[r], p[r + w].h, p[r + w].l);
-    const F2 mine = f2_warp_sum(p[0]);
-    if (lane == 0) red[i & 1][warp] = mine;
+    for (int j = 0; j < 3; ++j) rsum[j * kMbSumThreads + tid] = f2_val(R[j]);
+    hsum[warp * 32 + lane] = f2_val(hacc);
   }
-  __syncthreads();  // the last warp sums are in `red`; every copy has landed
-  if (warp == 0) mb_fold_chunk(red[(count - 1) & 1], blockIdx.x + (count - 1) * G, nh, lane, chunk_mass, hacc);
-  // Fold the rows in FP32 pairs; FP64 for the per-thread results, in the ring.
-  F2 T{0.f, 0.f};
-  F2 R[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll
-  for (int r = 0; r < kMbRows; ++r) {
-    f2_add(T, v[r].h, v[r].l);
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      if ((r >> j) & 1) f2_add(R[j], v[r].h, v[r].l);
-  }
-  double* tsum = reinterpret_cast<double*>(mb_smem);
-  double* rsum = tsum + kMbThreads;  // [3][kMbThreads]
-  tsum[tid] = f2_val(T);
-#pragma unroll
-  for (int j = 0; j < 3; ++j) rsum[j * kMbThreads + tid] = f2_val(R[j]);
   __syncthreads();
   double* out = partial + (int64_t)blockIdx.x * (n + 1);
   if (tid < kMbChunkBits) {
     double acc = 0.;
     if (tid < 9) {
-      for (int t = 0; t < kMbThreads; ++t)
+      for (int t = 0; t < kMbSumThreads; ++t)
         if ((t >> tid) & 1) acc += tsum[t];
     } else {
-      for (int t = 0; t < kMbThreads; ++t) acc += rsum[(tid - 9) * kMbThreads + t];
+      for (int t = 0; t < kMbSumThreads; ++t) acc += rsum[(tid - 9) * kMbSumThreads + t];
     }
     out[tid] = acc;
+  } else if (tid >= 32 && tid < 32 + nh) {
+    double acc = 0.;
+    for (int w = 0; w < kMbSumWarps; ++w) acc += hsum[w * 32 + (tid - 32)];
+    out[kMbChunkBits + (tid - 32)] = acc;
   } else if (tid == kMbThreads - 1) {
     double acc = 0.;
-    for (int t = 0; t < kMbThreads; ++t) acc += tsum[t];
+    for (int t = 0; t < kMbSumThreads; ++t) acc += tsum[t];
     out[n] = acc;
   }
-  if (warp == 0 && lane < nh) out[kMbChunkBits + lane] = f2_val(hacc);
 }
 
-// The sampler's segment prefixes for states of 12 or more qubits, staged as
-// in k_chunk_mass_bulk: 4096-amplitude chunks of 16 segments of 256; warp w
-// sums segment w (lane l: elements l + 32 r), warp 0 scans the 16 segment
-// masses of the previous chunk while the next one is summed. Outputs as
-// k_segment_prefix_f2 with seg_bits 8 and chunk_bits 12.
+// The sampler's segment masses for states of 12 or more qubits, staged as in
+// k_chunk_mass_bulk: 4096-amplitude chunks of 16 segments of 256; summing
+// warp w sums segment w of each chunk (lane l: elements l + 32 r) and writes
+// it to seg[c * 16 + w]. k_segment_scan then turns each chunk's 16 masses
+// into running sums and the chunk mass.
 constexpr int kSpSegBits = 8;
-static_assert((kMbChunkBits - kSpSegBits) == 4 && kMbWarps == 16, "one warp per segment");
-
-__device__ __forceinline__ void sp_fold_chunk(const F2* red, int64_t c, int lane, double* seg_incl,
-                                              double* chunk_mass) {
-  constexpr int spc = 1 << (kMbChunkBits - kSpSegBits);
-  F2 t = lane < spc ? red[lane] : F2{0.f, 0.f};
-#pragma unroll
-  for (int o = 1; o < spc; o <<= 1) {  // inclusive scan over lanes 0..15
-    const float h = __shfl_up_sync(0xffffffffu, t.h, o);
-    const float l = __shfl_up_sync(0xffffffffu, t.l, o);
-    if (lane >= o) {
-      F2 u{h, l};
-      f2_add(u, t.h, t.l);
-      t = u;
-    }
-  }
-  if (lane < spc) seg_incl[c * spc + lane] = f2_val(t);
-  if (lane == spc - 1) chunk_mass[c] = f2_val(t);
-}
+constexpr int kSpSegsPerChunk = 1 << (kMbChunkBits - kSpSegBits);
+static_assert(kSpSegsPerChunk == kMbSumWarps, "one summing warp per segment");
 
 template <int SRC>
 __global__ void __launch_bounds__(kMbThreads, 1)
-k_segment_prefix_bulk(const void* src, int64_t num_chunks, double* __restrict__ seg_incl,
-                      double* __restrict__ chunk_mass, uint32_t wait_limit, int* __restrict__ status) {
+k_segment_mass_bulk(const void* src, int64_t num_chunks, double* __restrict__ seg, uint32_t wait_limit,
+                    int* __restrict__ status) {
   using A = typename MbAmp<SRC>::T;
   constexpr int C = 1 << kMbChunkBits;
   extern __shared__ __align__(128) unsigned char mb_smem[];
   A* ring = reinterpret_cast<A*>(mb_smem);
-  __shared__ __align__(8) uint64_t full[kMbStages];
-  __shared__ F2 red[2][kMbWarps];
+  __shared__ __align__(8) BulkRing rb;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t G = gridDim.x;
   const int64_t count = (num_chunks - blockIdx.x + G - 1) / G;
-  const A* gsrc = static_cast<const A*>(src);
-  mb_start(ring, full, gsrc, count);
-  for (int64_t i = 0; i < count; ++i) {
-    const int s = (int)(i % kMbStages);
-    const bool ok = mbar_wait(&full[s], (uint32_t)((i / kMbStages) & 1), wait_limit);
-    A a[kMbRows];
+  ring_init(rb);
+  if (warp == kMbSumWarps) {
+    if (lane == 0) ring_produce(rb, ring, static_cast<const A*>(src), count, wait_limit, status);
+  } else {
+    for (int64_t i = 0; i < count; ++i) {
+      if (!ring_wait_full(rb, i, wait_limit, status)) break;
+      const A* buf = ring + (size_t)(i % kMbStages) * C + (warp << kSpSegBits);
+      A a[kMbRows];
 #pragma unroll
-    for (int r = 0; r < kMbRows; ++r) a[r] = ring[(size_t)s * C + (warp << kSpSegBits) + lane + 32 * r];
-    if (__syncthreads_or(!ok)) {
-      mb_give_up(full, i, count, status);
-      return;
-    }
-    if (tid == 0 && i + kMbStages < count) mb_issue(ring, full, gsrc, i + kMbStages);
-    if (warp == 0 && i > 0) sp_fold_chunk(red[(i - 1) & 1], blockIdx.x + (i - 1) * G, lane, seg_incl, chunk_mass);
-    F2 acc = mb_prob<SRC>(a[0]);
+      for (int r = 0; r < kMbRows; ++r) a[r] = buf[lane + 32 * r];
+      ring_release(rb, i);
+      F2 acc = mb_prob<SRC>(a[0]);
 #pragma unroll
-    for (int r = 1; r < kMbRows; ++r) {
-      const F2 p = mb_prob<SRC>(a[r]);
-      f2_add(acc, p.h, p.l);
+      for (int r = 1; r < kMbRows; ++r) {
+        const F2 p = mb_prob<SRC>(a[r]);
+        f2_add(acc, p.h, p.l);
+      }
+      acc = f2_warp_sum(acc);
+      if (lane == 0) seg[(blockIdx.x + i * G) * kSpSegsPerChunk + warp] = f2_val(acc);
     }
-    acc = f2_warp_sum(acc);
-    if (lane == 0) red[i & 1][warp] = acc;
   }
-  __syncthreads();
-  if (warp == 0) sp_fold_chunk(red[(count - 1) & 1], blockIdx.x + (count - 1) * G, lane, seg_incl, chunk_mass);
+  __syncthreads();  // the producer has seen its last copies land
+}
+
+// In place, per chunk c: seg[c * 16 + j] <- seg[c * 16] + ... + seg[c * 16 + j]
+// (FP64, in segment order), chunk_mass[c] <- the last of them.
+__global__ void k_segment_scan(double* __restrict__ seg, int64_t num_chunks, double* __restrict__ chunk_mass) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= num_chunks) return;
+  double* p = seg + c * kSpSegsPerChunk;
+  double run = 0.;
+#pragma unroll
+  for (int j = 0; j < kSpSegsPerChunk; ++j) {
+    run += p[j];
+    p[j] = run;
+  }
+  chunk_mass[c] = run;
 }
 
 // Sum the per-CTA partials in CTA order.
@@ -987,66 +927,56 @@ void mass_bulk_attributes() {
 }
 
 template <int SRC>
-void launch_mass_bulk(const void* src, int n, int64_t num_chunks, int grid, double* mass, double* partial,
-                      cudaStream_t stream) {
+void launch_mass_bulk(const void* src, int n, int64_t num_chunks, int grid, double* partial, cudaStream_t stream) {
   constexpr size_t smem = mass_bulk_smem<SRC>();
   mass_bulk_attributes<SRC>();
-  k_chunk_mass_bulk<SRC><<<grid, kMbThreads, smem, stream>>>(src, n, num_chunks, mass, partial, tma_wait_limit(),
+  k_chunk_mass_bulk<SRC><<<grid, kMbThreads, smem, stream>>>(src, n, num_chunks, partial, tma_wait_limit(),
                                                              tma_status_word());
 }
 
+// Segment masses (bulk-staged) and their per-chunk running sums.
 template <int SRC>
-void launch_prefix_bulk(const void* src, int64_t num_chunks, int grid, double* seg, double* mass,
-                        cudaStream_t stream) {
+void launch_segment_bulk(const void* src, int64_t num_chunks, int grid, double* seg, double* mass,
+                         cudaStream_t stream) {
   constexpr size_t smem = mass_bulk_smem<SRC>();
   static const cudaError_t attr =
-      cudaFuncSetAttribute(k_segment_prefix_bulk<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_segment_mass_bulk<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   (void)attr;  // a refusal shows as the launch's error
-  k_segment_prefix_bulk<SRC><<<grid, kMbThreads, smem, stream>>>(src, num_chunks, seg, mass, tma_wait_limit(),
-                                                                 tma_status_word());
+  k_segment_mass_bulk<SRC><<<grid, kMbThreads, smem, stream>>>(src, num_chunks, seg, tma_wait_limit(),
+                                                               tma_status_word());
+  k_segment_scan<<<(int)((num_chunks + 255) / 256), 256, 0, stream>>>(seg, num_chunks, mass);
 }
 
-// The per-chunk / per-bit mass pass: FP32 pairs for amplitudes (src_kind 0
-// complex128, 1 complex64), FP64 for a probability vector (src_kind 2).
-void launch_mass_kernel(const void* src, int src_kind, int n, int cb, int64_t num_chunks, int grid, double* mass,
+// The Pauli-Z mass pass over amplitudes (src_kind 0 complex128, 1
+// complex64): per CTA the n + 1 sums in `partial`.
+void launch_mass_kernel(const void* src, int src_kind, int n, int cb, int64_t num_chunks, int grid,
                         double* partial, cudaStream_t stream) {
   if (mass_uses_bulk(src_kind, n)) {
-    if (src_kind == 0) launch_mass_bulk<0>(src, n, num_chunks, grid, mass, partial, stream);
-    else launch_mass_bulk<1>(src, n, num_chunks, grid, mass, partial, stream);
-    return;
-  }
-  switch (src_kind) {
-    case 0: k_chunk_mass_f2<0><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
-    case 1: k_chunk_mass_f2<1><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
-    default: k_chunk_mass<2><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, mass, partial); break;
+    if (src_kind == 0) launch_mass_bulk<0>(src, n, num_chunks, grid, partial, stream);
+    else launch_mass_bulk<1>(src, n, num_chunks, grid, partial, stream);
+  } else if (src_kind == 0) {
+    k_chunk_mass_f2<0><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, partial);
+  } else {
+    k_chunk_mass_f2<1><<<grid, kRedThreads, 0, stream>>>(src, n, cb, num_chunks, partial);
   }
 }
 
-int grid_for_chunks(int64_t num_chunks) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>(num_chunks, (int64_t)sm_count() * 8));
-}
-
-// Runs k_chunk_mass and the partial reduction. Leaves chunk masses in
-// chunk_dev and the n+1 sums (bit-set mass per qubit, then total) in `sums_dev`.
-int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& chunk_dev,
-                    DeviceBuffer& reduce_dev, cudaStream_t stream, double** sums_dev_out,
-                    int64_t* num_chunks_out, int* chunk_bits_out) {
-  const int cb = src_kind == 2 ? chunk_bits_for(n) : mass_chunk_bits_for(n);
+// Runs the mass pass and the partial reduction. Leaves the n+1 sums
+// (bit-set mass per qubit, then total) in `sums_dev`.
+int chunk_mass_pass(const void* src, int src_kind, int n, DeviceBuffer& reduce_dev, cudaStream_t stream,
+                    double** sums_dev_out) {
+  const int cb = mass_chunk_bits_for(n);
   const int64_t num_chunks = int64_t(1) << (n - cb);
-  const int grid = src_kind == 2 ? grid_for_chunks(num_chunks) : mass_grid_for(src_kind, n, num_chunks);
-  DMV_TRY(chunk_dev.reserve((size_t)num_chunks * sizeof(double)));
+  const int grid = mass_grid_for(src_kind, n, num_chunks);
   const size_t partial_elems = (size_t)grid * (n + 1);
   DMV_TRY(reduce_dev.reserve((partial_elems + (size_t)(n + 1)) * sizeof(double)));
   double* partial = static_cast<double*>(reduce_dev.ptr);
   double* sums = partial + partial_elems;
-  double* mass = static_cast<double*>(chunk_dev.ptr);
-  launch_mass_kernel(src, src_kind, n, cb, num_chunks, grid, mass, partial, stream);
+  launch_mass_kernel(src, src_kind, n, cb, num_chunks, grid, partial, stream);
   k_reduce_partials<<<1, 64, 0, stream>>>(partial, n + 1, grid, sums);
   count_launch(2);
   DMV_CUDA_TRY(cudaGetLastError());
   *sums_dev_out = sums;
-  *num_chunks_out = num_chunks;
-  *chunk_bits_out = cb;
   return DMV_OK;
 }
 
@@ -1076,8 +1006,9 @@ int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefi
   int32_t* guide = reinterpret_cast<int32_t*>(seg + nseg);
   if (bulk) {
     const int grid = mass_grid_for(src_kind, n, sp.num_chunks);
-    if (src_kind == 0) launch_prefix_bulk<0>(src, sp.num_chunks, grid, seg, mass, stream);
-    else launch_prefix_bulk<1>(src, sp.num_chunks, grid, seg, mass, stream);
+    if (src_kind == 0) launch_segment_bulk<0>(src, sp.num_chunks, grid, seg, mass, stream);
+    else launch_segment_bulk<1>(src, sp.num_chunks, grid, seg, mass, stream);
+    count_launch(2);
   } else {
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 7) / 8, (int64_t)sm_count() * 8));
     switch (src_kind) {
@@ -1085,11 +1016,12 @@ int sample_prefix_pass(const void* src, int src_kind, int n, DeviceBuffer& prefi
       case 1: k_segment_prefix_f2<1><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
       default: k_segment_prefix<2><<<grid, kRedThreads, 0, stream>>>(src, sp.seg_bits, sp.chunk_bits, sp.num_chunks, seg, mass); break;
     }
+    count_launch();
   }
   k_scan_chunks<<<1, 1024, 0, stream>>>(mass, sp.num_chunks, incl);
   const int gg = (int)std::max<int64_t>(1, std::min<int64_t>((sp.num_chunks + 256) / 256, (int64_t)sm_count() * 4));
   k_chunk_guide<<<gg, 256, 0, stream>>>(incl, sp.num_chunks, sp.num_chunks, guide);
-  count_launch(3);
+  count_launch(2);
   DMV_CUDA_TRY(cudaGetLastError());
   sp.chunk_incl = incl;
   sp.guide = guide;
@@ -1140,11 +1072,12 @@ ChunkMassShape chunk_mass_shape(int n) {
   return sh;
 }
 
-int launch_chunk_mass_into(const void* src, int src_kind, int n, double* mass, double* partial, double* sums,
+int launch_chunk_mass_into(const void* src, int src_kind, int n, double* partial, double* sums,
                            cudaStream_t stream) {
-  if (src_kind == 2) return set_error(DMV_ERR_INVALID, "launch_chunk_mass_into takes amplitudes (kinds 0, 1)");
+  if (src_kind != 0 && src_kind != 1)
+    return set_error(DMV_ERR_INVALID, "launch_chunk_mass_into takes amplitudes (kinds 0, 1)");
   const ChunkMassShape sh = chunk_mass_shape(n);
-  launch_mass_kernel(src, src_kind, n, sh.chunk_bits, sh.num_chunks, sh.grid, mass, partial, stream);
+  launch_mass_kernel(src, src_kind, n, sh.chunk_bits, sh.num_chunks, sh.grid, partial, stream);
   k_reduce_partials<<<1, 64, 0, stream>>>(partial, n + 1, sh.grid, sums);
   count_launch(2);
   DMV_CUDA_TRY(cudaGetLastError());
@@ -1165,10 +1098,7 @@ int launch_probabilities(dmv_state_s* s, double* probs_device) {
 
 int launch_expect_z(dmv_state_s* s, double* expect_host, double* norm_host) {
   double* sums = nullptr;
-  int64_t nc = 0;
-  int cb = 0;
-  DMV_TRY(chunk_mass_pass(s->amps, s->precision == DMV_C128 ? 0 : 1, s->n, s->chunk_dev, s->reduce_dev,
-                          s->stream, &sums, &nc, &cb));
+  DMV_TRY(chunk_mass_pass(s->amps, s->precision == DMV_C128 ? 0 : 1, s->n, s->reduce_dev, s->stream, &sums));
   std::vector<double> h((size_t)s->n + 1);
   DMV_CUDA_TRY(cudaMemcpyAsync(h.data(), sums, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   DMV_CUDA_TRY(cudaStreamSynchronize(s->stream));
