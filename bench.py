@@ -309,6 +309,21 @@ def adjoint_section(args):
            "param_shift_grads_per_s": p.size / t_ps, "param_shift_sampled_params": int(k),
            "speedup_vs_param_shift": t_ps / t_adj, "max_abs_diff_vs_param_shift": float(np.max(np.abs(g[idx] - ps))),
            "loss": loss}
+    # The same sweep in the other complex128 arithmetics (psi and lambda updates in that
+    # arithmetic; FP32 pairs also form the gradient terms), checked against the FP64 gradient.
+    alts = {}
+    for arith in ("fp32x2", "int64"):
+        ca = Circuit(n, arithmetic=arith)
+        add_to_circuit(ca, gates)
+        ca.adjoint_gradient(w)  # warm-up
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            la, ga = ca.adjoint_gradient(w)
+        ta = (time.perf_counter() - t0) / reps
+        alts[arith] = {"adjoint_s": ta, "adjoint_grads_per_s": p.size / ta, "speedup_vs_fp64_adjoint": t_adj / ta,
+                       "max_abs_diff_vs_fp64_grads": float(np.max(np.abs(ga - g))), "loss_diff": abs(la - loss)}
+        del ca
+    out["alt_arithmetic"] = alts
     if not args.no_cpu:
         # The reference has no gradient; its route is parameter shift (circuit.rs:529-546):
         # two CPU forwards (clone per gate) per parameter. One loss evaluation timed here.

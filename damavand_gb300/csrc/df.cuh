@@ -163,6 +163,24 @@ __device__ __forceinline__ void df_apply_pair(const DFMat& m, float4& a0, float4
     df_finish(im, b1.z, b1.w);
     a0 = b0;
     a1 = b1;
+  } else if constexpr (CLS == OP_RXLIKE) {
+    // m00 = m[0], m11 = m[6] real; m01 = i m[3], m10 = i m[5]: four 2-term dots
+    DFAcc acc;
+    float4 b0, b1;
+    df_first(acc, m.h[0], m.l[0], a0.x, a0.y);  // m0 a0r - m3 a1i
+    df_add(acc, -m.h[3], -m.l[3], a1.z, a1.w);
+    df_finish(acc, b0.x, b0.y);
+    df_first(acc, m.h[0], m.l[0], a0.z, a0.w);  // m0 a0i + m3 a1r
+    df_add(acc, m.h[3], m.l[3], a1.x, a1.y);
+    df_finish(acc, b0.z, b0.w);
+    df_first(acc, -m.h[5], -m.l[5], a0.z, a0.w);  // -m5 a0i + m6 a1r
+    df_add(acc, m.h[6], m.l[6], a1.x, a1.y);
+    df_finish(acc, b1.x, b1.y);
+    df_first(acc, m.h[5], m.l[5], a0.x, a0.y);  // m5 a0r + m6 a1i
+    df_add(acc, m.h[6], m.l[6], a1.z, a1.w);
+    df_finish(acc, b1.z, b1.w);
+    a0 = b0;
+    a1 = b1;
   } else if constexpr (CLS == OP_REAL) {
     DFAcc acc;
     float4 b0, b1;

@@ -172,6 +172,7 @@ namespace {
 struct PGate {
   int32_t target, control;
   double m[8];
+  int32_t param, generator;  // adjoint tags (PlanOptions::param_of), else -1 / 0
 };
 
 Op make_op(const PGate& g, int32_t target_pos, int32_t ctrl, int32_t ctrl_kind) {
@@ -183,8 +184,8 @@ Op make_op(const PGate& g, int32_t target_pos, int32_t ctrl, int32_t ctrl_kind) 
   op.ctrl = ctrl;
   op.ctrl_kind = ctrl_kind;
   op.cls = classify(g.m);
-  op.param = -1;
-  op.generator = 0;
+  op.param = g.param;
+  op.generator = g.generator;
   return op;
 }
 
@@ -204,10 +205,12 @@ int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
   std::vector<PGate> fg;
   fg.reserve(gates.size());
   std::vector<int64_t> last_on((size_t)n, -1);
-  for (const Gate& g : gates) {
+  const bool tagged = opt.param_of != nullptr;
+  for (size_t gi = 0; gi < gates.size(); ++gi) {
+    const Gate& g = gates[gi];
     if (g.observable) continue;
     ++plan.num_gates;
-    if (opt.fusion != DMV_FUSE_NONE && g.control < 0) {
+    if (opt.fusion != DMV_FUSE_NONE && g.control < 0 && !tagged) {
       const int64_t j = last_on[(size_t)g.target];
       if (j >= 0 && fg[(size_t)j].control < 0 && fg[(size_t)j].target == g.target) {
         matmul2(g.m, fg[(size_t)j].m, fg[(size_t)j].m);
@@ -218,6 +221,8 @@ int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
     p.target = g.target;
     p.control = g.control;
     std::memcpy(p.m, g.m, sizeof(p.m));
+    p.param = tagged ? opt.param_of[gi] : -1;
+    p.generator = tagged && opt.generator_of ? opt.generator_of[gi] : 0;
     fg.push_back(p);
     last_on[(size_t)g.target] = (int64_t)fg.size() - 1;
     if (g.control >= 0) last_on[(size_t)g.control] = (int64_t)fg.size() - 1;

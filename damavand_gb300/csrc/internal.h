@@ -224,6 +224,10 @@ struct PlanOptions {
   int32_t tile_bits = 12;  // log2 amplitudes per tile
   int32_t low_bits = 6;    // always-local low qubits (coalesced chunks)
   bool windows_only = false;  // every pass a window pass (the batched kernel runs only those)
+  // Adjoint sweeps: when set, no gates are merged and the op made from
+  // gates[i] carries param_of[i] / generator_of[i] (Op::param, Op::generator).
+  const int32_t* param_of = nullptr;
+  const int32_t* generator_of = nullptr;
 };
 
 int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,

@@ -650,7 +650,7 @@ double op_multiply_adds(const Op& op, int64_t N, int arith) {
   const bool pair_arith = arith == ARITH_FP32X2, fixed = arith == ARITH_INT64;
   switch (op.cls) {
     case OP_GENERAL: per_pair = pair_arith ? 172. : fixed ? 64. : 16.; break;
-    case OP_RXLIKE: per_pair = pair_arith ? 172. : fixed ? 64. : 8.; break;  // general code in those arithmetics
+    case OP_RXLIKE: per_pair = pair_arith ? 76. : fixed ? 64. : 8.; break;  // int64: the general code
     case OP_SWAP: per_pair = 0.; break;
     case OP_ROT: per_pair = 6.; break;  // FP64 only: three shears on re and on im
     case OP_PHASE: per_pair = pair_arith ? 76. : fixed ? 32. : 6.; break;  // one complex product per amplitude

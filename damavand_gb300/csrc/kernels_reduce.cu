@@ -8,6 +8,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "complex_ops.cuh"
@@ -845,15 +846,57 @@ k_scale_z(V* __restrict__ dst, const V* __restrict__ src, int64_t N, const doubl
   }
 }
 
+// Im <l| P |p> over one pair (P the generator: 1 X, 2 Y, 3 Z) as a
+// compensated dot product of FP32 pairs (float4: re hi, re lo, im hi, im lo),
+// pre-update values.
+__device__ __forceinline__ F2 df_generator_term(int gen, const float4& p0, const float4& p1, const float4& l0,
+                                                const float4& l1) {
+  DFAcc a;
+  if (gen == 1) {  // l0r p1i - l0i p1r + l1r p0i - l1i p0r
+    df_first(a, l0.x, l0.y, p1.z, p1.w);
+    df_add(a, -l0.z, -l0.w, p1.x, p1.y);
+    df_add(a, l1.x, l1.y, p0.z, p0.w);
+    df_add(a, -l1.z, -l1.w, p0.x, p0.y);
+  } else if (gen == 2) {  // -l0r p1r - l0i p1i + l1r p0r + l1i p0i
+    df_first(a, -l0.x, -l0.y, p1.x, p1.y);
+    df_add(a, -l0.z, -l0.w, p1.z, p1.w);
+    df_add(a, l1.x, l1.y, p0.x, p0.y);
+    df_add(a, l1.z, l1.w, p0.z, p0.w);
+  } else {  // l0r p0i - l0i p0r - l1r p1i + l1i p1r
+    df_first(a, l0.x, l0.y, p0.z, p0.w);
+    df_add(a, -l0.z, -l0.w, p0.x, p0.y);
+    df_add(a, -l1.x, -l1.y, p1.z, p1.w);
+    df_add(a, l1.z, l1.w, p1.x, p1.y);
+  }
+  F2 r;
+  df_finish(a, r.h, r.l);
+  return r;
+}
+
+// In place: complex128 amplitudes -> the FP32-pair form (float4: re hi, re
+// lo, im hi, im lo; 16 bytes, like the double2 it replaces).
+__global__ void k_df_pack(double2* __restrict__ v, int64_t N) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride)
+    reinterpret_cast<float4*>(v)[i] = df_from_double2(v[i]);
+}
+
 // One step of the adjoint sweep for gate U (op holds U^dagger):
 //   grad += Im <lam| P |psi>   (P the rotation's generator, pre-update values)
 //   psi <- U^dagger psi, lam <- U^dagger lam.
-// The state updates use the state's arithmetic policy (FP64, FP32, FP32-pair);
-// the gradient term is always accumulated in FP64 from the loaded values.
-template <typename P>
+// The state updates use the state's arithmetic policy (FP64, FP32, FP32-pair,
+// int64 block fixed point). The gradient term is accumulated in FP64 from the
+// loaded values, except under FP32-pair arithmetic, where it is a compensated
+// FP32-pair dot product summed in FP32 pairs (FP64 once per thread): six FP64
+// operations per pair would otherwise cost as much as the pass's HBM traffic.
+// DF_RAW (FP32-pair only): psi and lam hold the FP32-pair form (k_df_pack)
+// and keep it, so no step converts (the conversions' integer work made the
+// step ALU-bound).
+template <typename P, bool DF_RAW = false>
 __global__ void __launch_bounds__(kRedThreads)
 k_adjoint_step(typename P::G* __restrict__ psi, typename P::G* __restrict__ lam,
                int64_t num_pairs, Op op, int apply, double* __restrict__ partial) {
+  static_assert(!DF_RAW || std::is_same<P, PolDF>::value, "the raw pair form is FP32-pair arithmetic's");
   using V = typename P::G;
   __shared__ double red[32];
   const typename P::Mat m = P::dmat(op);
@@ -863,10 +906,38 @@ k_adjoint_step(typename P::G* __restrict__ psi, typename P::G* __restrict__ lam,
   const int lo = ctrl ? min(t, c) : t, hi = ctrl ? max(t, c) : t;
   const int gen = op.generator;
   double acc = 0.;
+  F2 facc{0.f, 0.f};  // FP32-pair arithmetic's gradient sum
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < num_pairs; j += stride) {
     int64_t i0 = ctrl ? (insert_zero(insert_zero(j, lo), hi) | (int64_t(1) << c)) : insert_zero(j, t);
     const int64_t i1 = i0 | (int64_t(1) << t);
+    if constexpr (std::is_same<P, PolDF>::value) {
+      float4 q0, q1, m0, m1;
+      if constexpr (DF_RAW) {
+        float4* pf = reinterpret_cast<float4*>(psi);
+        float4* lf = reinterpret_cast<float4*>(lam);
+        q0 = pf[i0]; q1 = pf[i1]; m0 = lf[i0]; m1 = lf[i1];
+      } else {
+        q0 = P::in(psi[i0]); q1 = P::in(psi[i1]); m0 = P::in(lam[i0]); m1 = P::in(lam[i1]);
+      }
+      if (gen != 0) {
+        const F2 g = df_generator_term(gen, q0, q1, m0, m1);
+        f2_add(facc, g.h, g.l);
+      }
+      if (apply) {
+        apply_dyn<P>(op.cls, m, q0, q1);
+        apply_dyn<P>(op.cls, m, m0, m1);
+        if constexpr (DF_RAW) {
+          float4* pf = reinterpret_cast<float4*>(psi);
+          float4* lf = reinterpret_cast<float4*>(lam);
+          pf[i0] = q0; pf[i1] = q1; lf[i0] = m0; lf[i1] = m1;
+        } else {
+          psi[i0] = P::out(q0); psi[i1] = P::out(q1);
+          lam[i0] = P::out(m0); lam[i1] = P::out(m1);
+        }
+      }
+      continue;
+    }
     V p0 = psi[i0], p1 = psi[i1], l0 = lam[i0], l1 = lam[i1];
     if (gen != 0) {
       const double p0r = p0.x, p0i = p0.y, p1r = p1.x, p1i = p1.y;
@@ -897,9 +968,145 @@ k_adjoint_step(typename P::G* __restrict__ psi, typename P::G* __restrict__ lam,
     }
   }
   if (gen != 0) {
+    if constexpr (std::is_same<P, PolDF>::value) acc = f2_val(facc);
     acc = block_sum(acc, red);
     if (threadIdx.x == 0) partial[blockIdx.x] = acc;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Fused adjoint sweep in FP32-pair arithmetic: one launch per window of the
+// reversed gate list (the forward planner's windows, gates unmerged, each op
+// tagged with its parameter slot and generator). A CTA stages the tile of psi
+// and the tile of lambda (the same 2^k local indices, FP32-pair form, 2 x 64
+// KB), then runs the window's ops in order: for a rotation, every thread first
+// adds Im <lam| P |psi> over its pairs (pre-update values) to its FP32-pair
+// sum, folded per warp into a per-op, per-warp slot in shared memory; then the
+// pair updates of both tiles. The tiles go back to HBM once per window (4S
+// bytes per window instead of per gate). Reordering inside a window only
+// moves gates past gates on other qubits, which leaves every Im <lam| P |psi>
+// unchanged (V^dagger P V = P for V on other qubits).
+// ---------------------------------------------------------------------------
+constexpr int kAdjThreads = kTileThreads;  // 512
+constexpr int kAdjWarps = kAdjThreads / 32;
+constexpr int kAdjMaxOps = 256;  // ops per launch (a longer window runs as several launches)
+
+struct AdjWindowParams {
+  int32_t k, low, nh, num_ops;
+  int32_t high[16];
+  int64_t num_tiles;
+  const Op* ops;
+  double* partial;  // partial[param * cols + cta]
+  int64_t cols;
+};
+
+template <int CLS>
+__device__ __forceinline__ void adj_tile_op(float4* ps, float4* la, int T, const Op& op, F2& g) {
+  const DFMat m = PolDF::dmat(op);
+  const int t = op.target, gen = op.generator;
+  const bool lctrl = op.ctrl_kind == CTRL_LOCAL;
+  const int c = op.ctrl;
+  const int lo = lctrl ? min(t, c) : t, hi = lctrl ? max(t, c) : t;
+  const int pairs = lctrl ? (T >> 2) : (T >> 1);
+  for (int q = threadIdx.x; q < pairs; q += kAdjThreads) {
+    const uint32_t l0 = lctrl ? (insert_zero32(insert_zero32((uint32_t)q, lo), hi) | (1u << c))
+                              : insert_zero32((uint32_t)q, t);
+    const uint32_t l1 = l0 | (1u << t);
+    float4 p0 = ps[l0], p1 = ps[l1], m0 = la[l0], m1 = la[l1];
+    if (gen != 0) {
+      const F2 d = df_generator_term(gen, p0, p1, m0, m1);
+      f2_add(g, d.h, d.l);
+    }
+    PolDF::template apply<CLS>(m, p0, p1);
+    PolDF::template apply<CLS>(m, m0, m1);
+    ps[l0] = p0; ps[l1] = p1;
+    la[l0] = m0; la[l1] = m1;
+  }
+}
+
+__global__ void __launch_bounds__(kAdjThreads, 1)
+k_adjoint_window(float4* __restrict__ psi, float4* __restrict__ lam, const AdjWindowParams p) {
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  const int T = 1 << p.k;
+  float4* ps = reinterpret_cast<float4*>(adj_smem);
+  float4* la = ps + T;
+  F2* acc = reinterpret_cast<F2*>(la + T);  // [num_ops][kAdjWarps]
+  __shared__ int64_t s_slot[kMaxSlots];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < p.num_ops * kAdjWarps; i += kAdjThreads) acc[i] = F2{0.f, 0.f};
+  const int64_t t_off = tile_thread_offset(p.low, p.nh, p.high);
+  tile_slot_offsets(p.low, p.nh, p.high, (T + kTileThreads - 1) >> kTileThreadBits, s_slot);
+  __syncthreads();
+  for (int64_t tix = blockIdx.x; tix < p.num_tiles; tix += gridDim.x) {
+    int64_t base = tix << p.low;
+    for (int i = 0; i < p.nh; ++i) base = insert_zero(base, p.high[i]);
+    tile_load<PolRaw<PolDF>, false>(ps, psi, base, T, t_off, s_slot);
+    tile_load<PolRaw<PolDF>, false>(la, lam, base, T, t_off, s_slot);
+    __syncthreads();
+    for (int o = 0; o < p.num_ops; ++o) {
+      const Op& op = p.ops[o];
+      if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1)) continue;  // uniform per tile
+      F2 g{0.f, 0.f};
+      switch (op.cls) {
+        case OP_SWAP: adj_tile_op<OP_SWAP>(ps, la, T, op, g); break;
+        case OP_DIAG: adj_tile_op<OP_DIAG>(ps, la, T, op, g); break;
+        case OP_ANTI: adj_tile_op<OP_ANTI>(ps, la, T, op, g); break;
+        case OP_REAL: adj_tile_op<OP_REAL>(ps, la, T, op, g); break;
+        case OP_RXLIKE: adj_tile_op<OP_RXLIKE>(ps, la, T, op, g); break;
+        default: adj_tile_op<OP_GENERAL>(ps, la, T, op, g); break;
+      }
+      if (op.generator != 0) {
+        g = f2_warp_sum(g);
+        if (lane == 0) f2_add(acc[o * kAdjWarps + warp], g.h, g.l);
+      }
+      __syncthreads();
+    }
+    tile_store<PolRaw<PolDF>>(ps, psi, base, T, t_off, s_slot);
+    tile_store<PolRaw<PolDF>>(la, lam, base, T, t_off, s_slot);
+    __syncthreads();
+  }
+  // Per op, this CTA's sum over its tiles (warps in order; FP64 once).
+  for (int o = threadIdx.x; o < p.num_ops; o += kAdjThreads) {
+    const Op& op = p.ops[o];
+    if (op.generator == 0 || op.param < 0) continue;
+    F2 t{0.f, 0.f};
+    for (int w = 0; w < kAdjWarps; ++w) f2_add(t, acc[o * kAdjWarps + w].h, acc[o * kAdjWarps + w].l);
+    p.partial[(int64_t)op.param * p.cols + blockIdx.x] = f2_val(t);
+  }
+}
+
+size_t adjoint_window_smem(int k, int num_ops) {
+  return ((size_t)2 << k) * sizeof(float4) + (size_t)num_ops * kAdjWarps * sizeof(F2);
+}
+
+// Grid of k_adjoint_window: one CTA per SM (the two tiles take 128 KB).
+int adjoint_window_grid(int64_t num_tiles) { return (int)std::min<int64_t>(num_tiles, (int64_t)sm_count()); }
+
+int launch_adjoint_window(dmv_state_s* psi, dmv_state_s* lam, int32_t n, const Pass& ps, const Op* ops_dev,
+                          double* part, int64_t cols) {
+  AdjWindowParams p;
+  p.k = ps.low_bits + ps.num_high;
+  p.low = ps.low_bits;
+  p.nh = ps.num_high;
+  for (int i = 0; i < 16; ++i) p.high[i] = i < ps.num_high ? ps.high[i] : 0;
+  p.num_tiles = int64_t(1) << (n - p.k);
+  p.partial = part;
+  p.cols = cols;
+  const int grid = adjoint_window_grid(p.num_tiles);
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      k_adjoint_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adjoint_window_smem(12, kAdjMaxOps));
+  (void)attr;  // a refusal shows as the launch's error
+  for (int64_t o = 0; o < ps.op_count; o += kAdjMaxOps) {
+    p.ops = ops_dev + ps.op_begin + o;
+    p.num_ops = (int32_t)std::min<int64_t>(kAdjMaxOps, ps.op_count - o);
+    const int64_t tok = prof_begin(DMV_KERNEL_ADJOINT, psi->stream, 4.0 * (double)psi->amp_bytes());
+    k_adjoint_window<<<grid, kAdjThreads, adjoint_window_smem(p.k, p.num_ops), psi->stream>>>(
+        static_cast<float4*>(psi->amps), static_cast<float4*>(lam->amps), p);
+    prof_end(tok, psi->stream);
+    count_launch();
+  }
+  DMV_CUDA_TRY(cudaGetLastError());
+  return DMV_OK;
 }
 
 int chunk_bits_for(int n) { return std::min(kMaxChunkBits, n); }
@@ -1237,7 +1444,7 @@ int adjoint_grid(int64_t num_pairs) {
 }
 
 int launch_adjoint_step_impl(dmv_state_s* psi, dmv_state_s* lam, const Op& op, int apply,
-                             double* partial_slot) {
+                             double* partial_slot, bool df_raw = false) {
   const bool ctrl = op.ctrl_kind != CTRL_NONE && op.ctrl >= 0;
   const int64_t pairs = psi->N >> (ctrl ? 2 : 1);
   const int grid = adjoint_grid(pairs);
@@ -1249,6 +1456,9 @@ int launch_adjoint_step_impl(dmv_state_s* psi, dmv_state_s* lam, const Op& op, i
   else if ((psi->arith == ARITH_INT64 || psi->arith == ARITH_TC) && op.unitary)
     k_adjoint_step<PolFX><<<grid, kRedThreads, 0, psi->stream>>>(
         static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
+  else if (psi->arith == ARITH_FP32X2 && df_raw)
+    k_adjoint_step<PolDF, true><<<grid, kRedThreads, 0, psi->stream>>>(
+        static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
   else if (psi->arith == ARITH_FP32X2)
     k_adjoint_step<PolDF><<<grid, kRedThreads, 0, psi->stream>>>(
         static_cast<double2*>(psi->amps), static_cast<double2*>(lam->amps), pairs, op, apply, partial_slot);
@@ -1258,6 +1468,47 @@ int launch_adjoint_step_impl(dmv_state_s* psi, dmv_state_s* lam, const Op& op, i
   prof_end(tok, psi->stream);
   count_launch();
   DMV_CUDA_TRY(cudaGetLastError());
+  return DMV_OK;
+}
+
+// The reverse sweep over psi and lam in the FP32-pair form, fused into
+// windows: the gate list reversed, each gate replaced by U^dagger and tagged
+// with its parameter slot and generator, planned without merging; window
+// passes run k_adjoint_window, single-gate passes k_adjoint_step.
+int adjoint_sweep_windows(dmv_state_s* s, dmv_state_s* psi, dmv_state_s* lam, const std::vector<Gate>& gates,
+                          const std::vector<int64_t>& slot_of, double* part, int64_t cols, DeviceBuffer& ops_buf) {
+  std::vector<Gate> rev;
+  std::vector<int32_t> param, gen;
+  rev.reserve(gates.size());
+  for (int64_t gi = (int64_t)gates.size() - 1; gi >= 0; --gi) {
+    const Gate& g = gates[(size_t)gi];
+    if (g.observable) continue;
+    Gate h = g;
+    adjoint2(g.m, h.m);
+    rev.push_back(h);
+    param.push_back((int32_t)slot_of[(size_t)gi]);
+    gen.push_back(slot_of[(size_t)gi] >= 0 ? rotation_generator(g.kind) : 0);
+  }
+  PlanOptions opt = plan_options_for(s, DMV_FUSE_WINDOW);
+  opt.param_of = param.data();
+  opt.generator_of = gen.data();
+  Plan plan;
+  DMV_TRY(build_plan(rev, s->n, s->precision, opt, plan));
+  if (!plan.ops.empty()) {
+    DMV_TRY(ops_buf.reserve(plan.ops.size() * sizeof(Op)));
+    DMV_CUDA_TRY(cudaMemcpyAsync(ops_buf.ptr, plan.ops.data(), plan.ops.size() * sizeof(Op), cudaMemcpyHostToDevice,
+                                 s->stream));
+  }
+  const Op* ops_dev = static_cast<const Op*>(ops_buf.ptr);
+  for (const Pass& ps : plan.passes) {
+    if (ps.kind == 1) {
+      DMV_TRY(launch_adjoint_window(psi, lam, s->n, ps, ops_dev, part, cols));
+    } else {
+      const Op& op = plan.ops[(size_t)ps.op_begin];
+      double* slot = op.param >= 0 ? part + (size_t)op.param * cols : part;
+      DMV_TRY(launch_adjoint_step_impl(psi, lam, op, 1, slot, true));
+    }
+  }
   return DMV_OK;
 }
 
@@ -1287,10 +1538,12 @@ int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const doubl
   if (rc != DMV_OK) return rc;
   rc = dmv_state_create(s->n, s->precision, s->stream, &lam);
   if (rc != DMV_OK) { dmv_state_destroy(psi); return rc; }
+  psi->arith = lam->arith = s->arith;  // the sweep runs in the state's arithmetic
 
-  DeviceBuffer partial;
+  DeviceBuffer partial, adj_ops;
   const int64_t pairs_u = s->N >> 1;
-  const int grid = adjoint_grid(pairs_u);
+  // Columns of the per-parameter partials: the widest grid of the sweep's kernels.
+  const int grid = std::max(adjoint_grid(pairs_u), adjoint_window_grid(int64_t(1) << std::max(0, s->n - 12)));
   do {
     rc = partial.reserve((size_t)num_params * grid * sizeof(double) + (size_t)num_params * sizeof(double));
     if (rc != DMV_OK) break;
@@ -1306,7 +1559,20 @@ int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const doubl
     }
     rc = launch_scale_by_z_observable(lam, s, weights);
     if (rc != DMV_OK) break;
-    for (int64_t gi = (int64_t)gates.size() - 1; gi >= 0 && rc == DMV_OK; --gi) {
+    // FP32-pair arithmetic: psi and lam are scratch, so they take the pair form
+    // once and keep it for the whole sweep.
+    const bool df_raw = s->precision == DMV_C128 && s->arith == ARITH_FP32X2;
+    if (df_raw) {
+      const int pg = (int)std::max<int64_t>(1, std::min<int64_t>((s->N + 255) / 256, (int64_t)sm_count() * 8));
+      k_df_pack<<<pg, 256, 0, s->stream>>>(static_cast<double2*>(psi->amps), s->N);
+      k_df_pack<<<pg, 256, 0, s->stream>>>(static_cast<double2*>(lam->amps), s->N);
+      count_launch(2);
+    }
+    if (df_raw) {
+      rc = adjoint_sweep_windows(s, psi, lam, gates, slot_of, part, grid, adj_ops);
+      if (rc != DMV_OK) break;
+    }
+    for (int64_t gi = df_raw ? -1 : (int64_t)gates.size() - 1; gi >= 0 && rc == DMV_OK; --gi) {
       const Gate& g = gates[(size_t)gi];
       if (g.observable) continue;
       Op op;
@@ -1323,7 +1589,7 @@ int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const doubl
       // controlled parametrised gates use fewer CTAs and leave zeros behind.
       double* slot = op.param >= 0 ? part + (size_t)op.param * grid : part;
       const bool last = gi == 0;
-      rc = launch_adjoint_step_impl(psi, lam, op, last ? 0 : 1, slot);
+      rc = launch_adjoint_step_impl(psi, lam, op, last ? 0 : 1, slot, df_raw);
     }
     if (rc != DMV_OK) break;
     k_reduce_rows<<<(int)((num_params + 127) / 128), 128, 0, s->stream>>>(part, num_params, grid, out);
@@ -1336,6 +1602,7 @@ int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const doubl
   } while (false);
   cudaStreamSynchronize(s->stream);
   partial.release();
+  adj_ops.release();
   dmv_state_destroy(psi);
   dmv_state_destroy(lam);
   return rc;

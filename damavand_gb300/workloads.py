@@ -59,7 +59,9 @@ def loss_weights(n: int, seed: int) -> np.ndarray:
 
 def random_circuit(n: int, depth: int, rng: np.random.Generator, controlled_rotations: bool = False):
     """Random layers: one gate from {H,X,Y,Z,RX,RY,RZ} per qubit, then CNOTs over a
-    random floor(n/2)-qubit subset paired up (the batched configuration's shape)."""
+    random floor(n/2)-qubit subset paired up (the batched configuration's shape).
+    With `controlled_rotations`, each layer then adds RX/RY/RZ gates controlled
+    across another random pairing (the layers' draws are otherwise unchanged)."""
     gates = []
     for _ in range(depth):
         for q in range(n):
@@ -71,6 +73,11 @@ def random_circuit(n: int, depth: int, rng: np.random.Generator, controlled_rota
             sub = rng.permutation(n)[:m]
             for i in range(0, m, 2):
                 gates.append((CNOT, int(sub[i + 1]), int(sub[i]), False, 0.0))
+            if controlled_rotations:
+                sub = rng.permutation(n)[:m]
+                for i in range(0, m, 2):
+                    kind = PARAMETRISED[int(rng.integers(0, 3))]
+                    gates.append((kind, int(sub[i + 1]), int(sub[i]), False, float(rng.uniform(0.0, 2.0 * math.pi))))
     return gates
 
 

@@ -90,3 +90,15 @@ def apply_gates(st, gates, fusion=1):
     from damavand_gb300.workloads import gate_array
     arr, count = gate_array(gates)
     check(lib.dmv_apply_gates(st.handle, arr, count, fusion))
+
+
+def oracle_forward_any_control(oracle_mod, n, gates, psi=None):
+    """The oracle's pair update gate by gate with every gate's control honoured: the
+    library accepts a control on any gate kind, where the reference's forward (and so
+    oracle.forward) controls only CNOT."""
+    state = oracle_mod.zero_state(n) if psi is None else np.array(psi, dtype=np.complex128, copy=True)
+    for kind, target, control, obs, theta in gates:
+        if obs:
+            continue
+        oracle_mod.apply_gate_inplace(state, n, oracle_mod.gate_matrix(kind, theta), control, target)
+    return state

@@ -14,12 +14,15 @@ def _ansatz(n, layers, seed):
     return gates, parameters(gates), loss_weights(n, seed + 1)
 
 
+@pytest.mark.parametrize("arith", ["fp64", "fp32x2", "int64", "tc"])
 @pytest.mark.parametrize("n,layers", [(2, 2), (5, 3), (8, 2)])
-def test_adjoint_matches_oracle_param_shift(built_lib, oracle_mod, n, layers):
+def test_adjoint_matches_oracle_param_shift(built_lib, oracle_mod, n, layers, arith):
+    """The sweep runs in the circuit's complex128 arithmetic (psi and lambda updates;
+    under FP32 pairs the gradient terms too)."""
     from damavand_gb300 import Circuit
     from damavand_gb300.workloads import add_to_circuit
     gates, params, w = _ansatz(n, layers, seed=20 + n)
-    c = Circuit(n)
+    c = Circuit(n, arithmetic=arith)
     add_to_circuit(c, gates)
     loss, g = c.adjoint_gradient(w)
     og = [(k, t, cc, int(o), th) for k, t, cc, o, th in gates]
@@ -138,3 +141,68 @@ def test_autograd_forward_runs_no_sweep_and_keeps_device_tensors(built_lib, orac
     ez = oracle_mod.expect_z(oracle_mod.measure(oracle_mod.forward(n, og)))
     assert np.max(np.abs(wt.grad.cpu().numpy() - ez)) < 1e-6  # float32 gradient
     assert abs(L.item() - oracle_mod.loss(n, og, params, w32)) < 1e-12
+
+
+def test_adjoint_controlled_rotations_match_central_differences(built_lib):
+    """Controlled rotations (a control on RX/RY/RZ: the library's extension): the
+    gradient over the control-set half against FP64 central differences of the GPU loss."""
+    from damavand_gb300 import Circuit
+    from damavand_gb300.workloads import add_to_circuit, parameters, random_circuit
+    rng = np.random.default_rng(81)
+    n = 6
+    gates = random_circuit(n, 4, rng, controlled_rotations=True)
+    assert any(k in (4, 5, 6) and c >= 0 for k, _, c, _, _ in gates)
+    w = rng.standard_normal(n)
+    c = Circuit(n)
+    add_to_circuit(c, gates)
+    _, g = c.adjoint_gradient(w)
+    p = parameters(gates)
+    h = 1e-6
+    fd = np.empty_like(p)
+    for j in range(p.size):
+        up, dn = p.copy(), p.copy()
+        up[j] += h
+        dn[j] -= h
+        c.set_parameters(up)
+        lu = c.loss(w)
+        c.set_parameters(dn)
+        fd[j] = (lu - c.loss(w)) / (2 * h)
+    c.set_parameters(p)
+    assert np.max(np.abs(g - fd)) < 5e-9
+
+
+@pytest.mark.parametrize("n,depth", [(14, 8), (18, 6)])
+def test_fp32x2_fused_sweep_on_mixed_gates_matches_fp64(built_lib, n, depth):
+    """The FP32-pair sweep runs fused windows: random layers with H, Paulis, rotations,
+    CNOTs and controlled rotations whose controls fall inside and outside the windows,
+    against the FP64 per-gate sweep."""
+    from damavand_gb300 import Circuit
+    from damavand_gb300.workloads import add_to_circuit, random_circuit
+    rng = np.random.default_rng(70 + n)
+    gates = random_circuit(n, depth, rng, controlled_rotations=True) + [(3, 2, -1, True, 0.0)]
+    w = rng.standard_normal(n)
+    ref = Circuit(n)
+    add_to_circuit(ref, gates)
+    l64, g64 = ref.adjoint_gradient(w)
+    c = Circuit(n, arithmetic="fp32x2")
+    add_to_circuit(c, gates)
+    loss, g = c.adjoint_gradient(w)
+    assert g.size > 0 and abs(loss - l64) < 1e-12
+    assert np.max(np.abs(g - g64)) < GRAD_ATOL
+
+
+@pytest.mark.parametrize("arith", ["fp32x2", "int64"])
+def test_adjoint_other_arithmetics_match_fp64_at_16_qubits(built_lib, arith):
+    """A 16-qubit, 4-layer ring ansatz (256 parameters): the FP32-pair and int64 sweeps
+    against the FP64 sweep, within the parameter-shift tolerance."""
+    from damavand_gb300 import Circuit
+    from damavand_gb300.workloads import add_to_circuit
+    gates, params, w = _ansatz(16, 4, seed=61)
+    ref = Circuit(16)
+    add_to_circuit(ref, gates)
+    l64, g64 = ref.adjoint_gradient(w)
+    c = Circuit(16, arithmetic=arith)
+    add_to_circuit(c, gates)
+    loss, g = c.adjoint_gradient(w)
+    assert abs(loss - l64) < 1e-12
+    assert g.shape == g64.shape and np.max(np.abs(g - g64)) < GRAD_ATOL
