@@ -42,8 +42,9 @@ sys.path.insert(0, REPO)
 
 METRIC = "30-qubit gate applies/s + HBM GB/s; adjoint vs param-shift grads/s at 1e-10"
 UNIT = "gate-applies/s"
-DTYPES = {"fp64": "f64 (complex128 storage, IEEE FP64 arithmetic; fused passes as real rotations applied as "
-                  "three shears and per-amplitude phase tables)",
+DTYPES = {"fp64": "f64 (complex128 storage, IEEE FP64 arithmetic; fused passes as real rotations, one "
+                  "multiply-add per output with their factors multiplied back once, and per-amplitude phase "
+                  "tables)",
           "fp64-direct": "f64 (complex128 storage, IEEE FP64 arithmetic; every fused 2x2 as a full complex "
                          "multiply-add)",
           "fp32x2": "f32x2 (complex128 storage, FP32-pair arithmetic, ~48-bit)",
@@ -839,7 +840,7 @@ def main():
     ap.add_argument("--no-alt", action="store_true",
                     help="skip the other complex128 arithmetics (timed and checked against FP64)")
     ap.add_argument("--arith", choices=["fp64", "fp64-direct", "fp32x2", "int64", "tc"], default="fp64",
-                    help="complex128 arithmetic: IEEE FP64 (rotations as shears and phase tables, or every 2x2 "
+                    help="complex128 arithmetic: IEEE FP64 (rotations and phase tables, or every 2x2 "
                          "as a full complex multiply-add), FP32 pairs (error-free transformations), "
                          "int64 block fixed point, or the same with dense blocks on the tensor cores")
     ap.add_argument("--no-adjoint", action="store_true")

@@ -90,7 +90,7 @@ class Circuit:
 
     def set_arithmetic(self, arithmetic: str) -> None:
         """Arithmetic on the complex128 amplitudes (complex64 ignores it): 'fp64' (IEEE FP64;
-        fused passes apply rotations and phase tables as shears), 'fp64-direct' (IEEE FP64,
+        fused passes apply real rotations and phase tables), 'fp64-direct' (IEEE FP64,
         every fused 2x2 as a full complex multiply-add), 'fp32x2' (FP32-pair error-free
         arithmetic, ~1e-13 normwise on deep circuits), 'int64' (block fixed point with exact
         integer products) or 'tc' (the same block fixed point, fused gates applied as dense

@@ -10,9 +10,13 @@
 //    D1 = diag(e^{i arg a}, e^{i arg c}), g = arg b + pi - arg a. The
 //    product is checked against U entry by entry; an op it does not
 //    reproduce to 4e-15 stays as it was. R acts on the real parts and the
-//    imaginary parts of a pair as the same real rotation, and a rotation is
-//    three shears, x0 += T x1, x1 += S x0, x0 += T x1 (T = -tan(t/2),
-//    S = sin t): 3 multiply-adds per amplitude instead of 8.
+//    imaginary parts of a pair as the same real rotation, applied as f M with
+//    M = [[1, -w], [w, 1]] (w = tan t, f = cos t) when cos t >= sin t, else
+//    M = [[w, -1], [1, w]] (w = cot t, f = sin t): each output is one
+//    multiply-add, 2 per amplitude instead of 8. The kernels apply M only; the
+//    product of the factors f (each >= 1/sqrt 2) is multiplied back into the
+//    state once, by the caller (three shears, x0 += T x1, x1 += S x0,
+//    x0 += T x1, keep the norm but cost 3 multiply-adds per amplitude).
 //  * Diagonal factors are not applied where they occur. Each is a phase per
 //    amplitude that depends on a few tile bits. Moving a diagonal later in
 //    time past an exchange (X, CNOT: a permutation P of the tile) re-indexes
@@ -30,8 +34,8 @@
 //    multiplies by i^q with a swap and sign flips on the integer pipe.
 //
 // On the 30-qubit ladder forward (600 fused single-qubit unitaries in 85
-// passes) this takes the FP64 work from 4800 to about 2650 multiply-adds
-// per amplitude (600 rotations and about 284 tables).
+// passes) this takes the FP64 work from 4800 to about 1900 multiply-adds
+// per amplitude (600 rotations at 2 and 238 tables at 3).
 #include <cmath>
 #include <algorithm>
 #include <cstring>
@@ -230,8 +234,8 @@ void phase_tables_fx(const std::vector<PhaseEntry>& in, std::vector<int4>& out) 
   }
 }
 
-int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool shears, std::vector<Op>& dst,
-                               std::vector<PhaseEntry>& tab) {
+int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool rot_ops, std::vector<Op>& dst,
+                               std::vector<PhaseEntry>& tab, ScaleDD* scale) {
   const int T = 1 << k;
   std::vector<DiagTable> tables;  // flushes in time order; tables[0] may sit at the pass start
   bool start_table = false;
@@ -310,10 +314,20 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool she
         r.target = t;
         r.ctrl = -1;
         r.ctrl_kind = CTRL_NONE;
-        if (shears) {
+        if (rot_ops) {
+          // R = f M with one entry pair of M exactly 1: two multiply-adds per
+          // component instead of three shears; f (>= 1/sqrt 2) goes to *scale.
+          (void)Tq;
           r.cls = OP_ROT;
-          r.m[0] = Tq;
-          r.m[1] = Sq;
+          if (Cq >= Sq) {
+            r.m[0] = Sq / Cq;
+            r.m[1] = 0.0;
+            if (scale) scale->mul(Cq);
+          } else {
+            r.m[0] = Cq / Sq;
+            r.m[1] = 1.0;
+            if (scale) scale->mul(Sq);
+          }
         } else {  // the rotation as a real 2x2 in the arithmetic's own form
           r.cls = OP_REAL;
           r.m[0] = Cq;
@@ -443,13 +457,15 @@ void host_op(std::vector<Cx>& tile, int k, const Op& op, const std::vector<Phase
     const uint32_t l1 = l0 | tb;
     Cx a0 = tile[l0], a1 = tile[l1];
     if (op.cls == OP_ROT) {
-      const double Tq = op.m[0], Sq = op.m[1];
-      double x0 = a0.re, x1 = a1.re, y0 = a0.im, y1 = a1.im;
-      x0 = std::fma(Tq, x1, x0); y0 = std::fma(Tq, y1, y0);
-      x1 = std::fma(Sq, x0, x1); y1 = std::fma(Sq, y0, y1);
-      x0 = std::fma(Tq, x1, x0); y0 = std::fma(Tq, y1, y0);
-      tile[l0] = Cx{x0, y0};
-      tile[l1] = Cx{x1, y1};
+      const double w = op.m[0];
+      const double x0 = a0.re, x1 = a1.re, y0 = a0.im, y1 = a1.im;
+      if (op.m[1] == 0.0) {
+        tile[l0] = Cx{std::fma(-w, x1, x0), std::fma(-w, y1, y0)};
+        tile[l1] = Cx{std::fma(w, x0, x1), std::fma(w, y0, y1)};
+      } else {
+        tile[l0] = Cx{std::fma(w, x0, -x1), std::fma(w, y0, -y1)};
+        tile[l1] = Cx{std::fma(w, x1, x0), std::fma(w, y1, y0)};
+      }
     } else {
       const double* m = op.m;
       tile[l0] = Cx{m[0] * a0.re - m[1] * a0.im + m[2] * a1.re - m[3] * a1.im,
@@ -490,10 +506,11 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
     const int k = ps.low_bits + ps.num_high;
     if (k != 12 || ps.num_high < 3) continue;
     ++n_passes;
-    for (int form = 0; form < 2; ++form) {  // rotations as shears (FP64), then as real 2x2 ops
+    for (int form = 0; form < 2; ++form) {  // rotations as OP_ROT (FP64), then as real 2x2 ops
     std::vector<Op> rw;
     std::vector<PhaseEntry> tab;
-    rewrite_pass_rotations(plan.ops.data() + ps.op_begin, ps.op_count, k, form == 0, rw, tab);
+    ScaleDD scale;
+    rewrite_pass_rotations(plan.ops.data() + ps.op_begin, ps.op_count, k, form == 0, rw, tab, &scale);
     if (form == 0)
       for (const Op& o : rw) {
         n_rot += o.cls == OP_ROT;
@@ -515,6 +532,7 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
       // emulation reads them from `base`, as the kernel does
       for (int64_t o = 0; o < ps.op_count; ++o) host_op(a, k, plan.ops[(size_t)(ps.op_begin + o)], tab, base);
       for (const Op& o : rw) host_op(b, k, o, tab, base, form == 1);
+      for (Cx& v : b) v = Cx{v.re * scale.hi, v.im * scale.hi};  // the rotations' factors
       double num = 0.0, den = 0.0;
       for (size_t i = 0; i < a.size(); ++i) {
         num = std::max(num, std::hypot(a[i].re - b[i].re, a[i].im - b[i].im));

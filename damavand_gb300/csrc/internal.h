@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <cmath>
 #include <vector>
 
 #include "../../include/damavand_gpu.h"
@@ -62,7 +63,9 @@ enum OpClass : int32_t {
   OP_ANTI = 4,     // m00 = m11 = 0 (Y and scaled exchanges)
   OP_RXLIKE = 5,   // m00, m11 real and m01, m10 imaginary (RX and its adjoint): 8 multiply-adds
   // Only in window passes rewritten by rewrite_pass_rotations (diag_plan.cpp):
-  OP_ROT = 6,      // FP64: real rotation [[c, -s], [s, c]] as three shears: m[0] = -tan(theta/2), m[1] = sin(theta)
+  OP_ROT = 6,      // FP64: real rotation R = [[c, -s], [s, c]] applied as f * M, two multiply-adds per component:
+                   //   m[1] == 0: M = [[1, -w], [w, 1]] (w = s/c, f = c); m[1] == 1: M = [[w, -1], [1, w]] (w = c/s, f = s);
+                   //   m[0] = w. The state is left divided by f; the caller multiplies the product of the f's back.
   OP_PHASE = 7     // every amplitude times a phase from a table (PhaseEntry); fields below
 };
 
@@ -149,19 +152,40 @@ void split_matrix(Op& op);
 
 // Rewrites the ops src[0 .. count) of one FP64 window pass over a tile of
 // 2^k amplitudes so that it spends fewer FP64 operations: every uncontrolled
-// unitary 2x2 becomes D1 R D2 (R a real rotation, applied as three shears;
-// D1, D2 diagonal), and the diagonal factors of the whole pass (with Z-type
+// unitary 2x2 becomes D1 R D2 (R a real rotation; D1, D2 diagonal), and the
+// diagonal factors of the whole pass (with Z-type
 // and controlled-phase ops and the diagonals of Y-type ops) are collected
 // into as few per-amplitude phase tables as the rotations allow: a diagonal
 // factor moves later in time through exchanges (re-indexed) and through
 // rotations on other bits, and earlier into the last table when nothing in
 // between touches its bits. Appends the new ops to `dst` and the tables to
 // `tab`; returns the number of ops appended.
-// `shears` true: rotations as OP_ROT (three shears, the FP64 kernels); false:
-// as OP_REAL 2x2 ops (with their FP32-pair, Q.54 and FP32 forms), for the
-// other arithmetics, which read the tables converted by phase_entry_value.
-int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool shears, std::vector<Op>& dst,
-                               std::vector<PhaseEntry>& tab);
+// `rot_ops` true: rotations as OP_ROT (the FP64 kernels: two multiply-adds
+// per component, the state left divided by each rotation's factor f, whose
+// product over the pass is multiplied into *scale); false: as OP_REAL 2x2 ops
+// (with their FP32-pair, Q.54 and FP32 forms), for the other arithmetics,
+// which read the tables converted by phase_entry_value.
+// A product of many factors kept to about 2^-100 relative (error-free
+// products through fma), for the OP_ROT factors.
+struct ScaleDD {
+  double hi = 1.0, lo = 0.0;
+  void mul(double f) {
+    const double p = hi * f;
+    const double e = std::fma(hi, f, -p);
+    const double l = std::fma(lo, f, e);
+    hi = p + l;
+    lo = l - (hi - p);
+  }
+  void mul(const ScaleDD& o) {
+    const double p = hi * o.hi;
+    const double e = std::fma(hi, o.hi, -p);
+    const double l = std::fma(hi, o.lo, std::fma(lo, o.hi, e));
+    hi = p + l;
+    lo = l - (hi - p);
+  }
+};
+int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool rot_ops, std::vector<Op>& dst,
+                               std::vector<PhaseEntry>& tab, ScaleDD* scale = nullptr);
 // e^{i phi} of a table entry in double.
 void phase_entry_value(const PhaseEntry& e, double& re, double& im);
 // The tables in the FP32-pair form (re_h, re_l, im_h, im_l) and as Q.54 limbs
@@ -311,6 +335,7 @@ struct dmv_state_s {
   std::vector<dmv::PhaseOp> phase_ops;   // compact ops of the register-phase launches
   dmv::DeviceBuffer phase_ops_dev;
   std::vector<dmv::PhaseEntry> phase_tab;  // phase tables of the rewritten passes
+  std::vector<dmv::ScaleDD> pass_scale;  // launch_plan: OP_ROT factor product per staged pass
   dmv::DeviceBuffer phase_tab_dev;
   std::vector<float4> phase_tab_df;        // the same tables for the FP32-pair arithmetic
   std::vector<int4> phase_tab_fx;          // and for the int64 arithmetic
@@ -344,6 +369,8 @@ inline PlanOptions plan_options_for(const dmv_state_s* s, int32_t fusion) {
 
 // Kernel launchers (kernels_*.cu). All stream-ordered on s->stream.
 int launch_set_zero(dmv_state_s* s);
+// The state times a real factor (complex128).
+int launch_scale_state(dmv_state_s* s, double f);
 int launch_plan(dmv_state_s* s, const Plan& plan);
 int launch_probabilities(dmv_state_s* s, double* probs_device);
 int launch_expect_z(dmv_state_s* s, double* expect_host, double* norm_host);

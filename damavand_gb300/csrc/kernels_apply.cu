@@ -652,7 +652,7 @@ double op_multiply_adds(const Op& op, int64_t N, int arith) {
     case OP_GENERAL: per_pair = pair_arith ? 172. : fixed ? 64. : 16.; break;
     case OP_RXLIKE: per_pair = pair_arith ? 76. : fixed ? 64. : 8.; break;  // int64: the general code
     case OP_SWAP: per_pair = 0.; break;
-    case OP_ROT: per_pair = 6.; break;  // FP64 only: three shears on re and on im
+    case OP_ROT: per_pair = 4.; break;  // FP64 only: one multiply-add per output, re and im
     case OP_PHASE: per_pair = pair_arith ? 76. : fixed ? 32. : 6.; break;  // one complex product per amplitude
     default: per_pair = pair_arith ? 76. : fixed ? 32. : 8.; break;
   }
@@ -683,8 +683,11 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   const bool c128 = s->precision == DMV_C128;
   const bool rewrite = c128 && ((s->arith == ARITH_FP64 && s->fp64_rewrite) || s->arith == ARITH_FP32X2 ||
                                 s->arith == ARITH_INT64);
-  const bool shears = s->arith == ARITH_FP64;
+  const bool rot_ops = s->arith == ARITH_FP64;
   s->phase_tab.clear();
+  // Per staged pass, the product of its OP_ROT factors (1 elsewhere).
+  std::vector<ScaleDD>& pass_scale = s->pass_scale;
+  pass_scale.clear();
   for (const Pass& ps : plan.passes) {
     const int rb = ps.kind == 1 ? window_reg_bits(s, ps) : 0;
     any_window |= ps.kind == 1;
@@ -692,13 +695,16 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
       Pass rw = ps;
       rw.op_begin = (int64_t)ops.size();
       std::vector<Op> src(plan.ops.begin() + ps.op_begin, plan.ops.begin() + ps.op_begin + ps.op_count);
+      ScaleDD f;
       rw.op_count =
-          rewrite_pass_rotations(src.data(), ps.op_count, ps.low_bits + ps.num_high, shears, ops, s->phase_tab);
+          rewrite_pass_rotations(src.data(), ps.op_count, ps.low_bits + ps.num_high, rot_ops, ops, s->phase_tab, &f);
       passes.push_back(rw);
+      pass_scale.push_back(f);
       continue;
     }
     if (rb <= 0) {
       passes.push_back(ps);
+      pass_scale.push_back(ScaleDD());
       continue;
     }
     any_phases = true;
@@ -708,6 +714,7 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
       sub.op_count = std::min<int64_t>(kMaxPhaseOps, ps.op_count - o);
       assign_phases(ops.data() + sub.op_begin, sub.op_count, ps.low_bits + ps.num_high, rb);
       passes.push_back(sub);
+      pass_scale.push_back(ScaleDD());
     }
   }
   if (any_window) DMV_TRY(upload_ops(s, ops.data(), (int64_t)ops.size()));
@@ -793,7 +800,18 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   // the FP32-pair form between them (k_apply_window's FMT bits).
   bool df_chain = c128 && s->arith == ARITH_FP32X2 && passes.size() >= 2;
   for (const Pass& ps : passes) df_chain = df_chain && ps.kind == 1;
+  // The OP_ROT factors left out of the state so far (each in [1/sqrt 2, 1]):
+  // multiplied back at the end, or earlier before the stored values could
+  // grow past 2^300.
+  ScaleDD owed;
   for (size_t pi = 0; pi < passes.size(); ++pi) {
+    if (pi > 0) {
+      owed.mul(pass_scale[pi - 1]);
+      if (std::fabs(owed.hi) < 0x1p-300) {
+        DMV_TRY(launch_scale_state(s, owed.hi));
+        owed = ScaleDD();
+      }
+    }
     const Pass& ps = passes[pi];
     const int df_fmt = df_chain ? ((pi > 0 ? 1 : 0) | (pi + 1 < passes.size() ? 2 : 0)) : 0;
     if (tc && tc_first[pi] >= 0) {
@@ -843,6 +861,10 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     }
     count_launch();
   }
+  if (!passes.empty()) {
+    owed.mul(pass_scale.back());
+  }
+  if (owed.hi != 1.0 || owed.lo != 0.0) DMV_TRY(launch_scale_state(s, owed.hi + owed.lo));
   DMV_CUDA_TRY(cudaGetLastError());
   s->last_tc_passes = s->last_tc_blocks = s->last_tc_swaps = 0;
   for (size_t pi = 0; pi < passes.size(); ++pi)
@@ -858,6 +880,24 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
                          (any_phases ? (int64_t)(s->phase_ops.size() * sizeof(PhaseOp)) : 0) +
                          (tc ? (int64_t)(s->tc_stages.size() * sizeof(TcStage) + s->tc_u.size() * 2) : 0);
   s->last_bytes = bytes;
+  return DMV_OK;
+}
+
+// The state times a real factor: the product of the FP64 rotations' factors
+// (OP_ROT) that the window passes leave out.
+__global__ void k_scale_state(double2* __restrict__ a, int64_t N, double f) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    const double2 v = a[i];
+    a[i] = make_double2(v.x * f, v.y * f);
+  }
+}
+
+int launch_scale_state(dmv_state_s* s, double f) {
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((s->N + 255) / 256, (int64_t)num_sms() * 8));
+  k_scale_state<<<grid, 256, 0, s->stream>>>(static_cast<double2*>(s->amps), s->N, f);
+  count_launch();
+  DMV_CUDA_TRY(cudaGetLastError());
   return DMV_OK;
 }
 

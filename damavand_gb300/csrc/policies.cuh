@@ -318,24 +318,24 @@ __device__ __forceinline__ void tile_op(typename P::T* tile, int T, const Op& op
 
 // OP_ROT (FP64 window passes): the real rotation [[c, -s], [s, c]] of every
 // pair along op.target, on the real parts and on the imaginary parts, as
-// three shears: x0 += T x1, x1 += S x0, x0 += T x1 with T = -tan(t/2) =
-// op.m[0], S = sin t = op.m[1] (3 multiply-adds per amplitude). Two pairs per
-// iteration, as in tile_op.
-__device__ __forceinline__ void rot_pair(double Tq, double Sq, double2& a0, double2& a1) {
-  double x0 = a0.x, x1 = a1.x, y0 = a0.y, y1 = a1.y;
-  x0 = fma(Tq, x1, x0);
-  y0 = fma(Tq, y1, y0);
-  x1 = fma(Sq, x0, x1);
-  y1 = fma(Sq, y0, y1);
-  x0 = fma(Tq, x1, x0);
-  y0 = fma(Tq, y1, y0);
-  a0 = make_double2(x0, y0);
-  a1 = make_double2(x1, y1);
+// f M: M = [[1, -w], [w, 1]] (op.m[1] == 0) or [[w, -1], [1, w]] (op.m[1] ==
+// 1), w = op.m[0]; one multiply-add per output (2 per amplitude). The factor
+// f is not applied here: the plan multiplies the product of its rotations'
+// factors back into the state once. Two pairs per iteration, as in tile_op.
+template <bool FORM_B>
+__device__ __forceinline__ void rot_pair(double w, double2& a0, double2& a1) {
+  const double x0 = a0.x, x1 = a1.x, y0 = a0.y, y1 = a1.y;
+  if constexpr (!FORM_B) {
+    a0 = make_double2(fma(-w, x1, x0), fma(-w, y1, y0));
+    a1 = make_double2(fma(w, x0, x1), fma(w, y0, y1));
+  } else {
+    a0 = make_double2(fma(w, x0, -x1), fma(w, y0, -y1));
+    a1 = make_double2(fma(w, x1, x0), fma(w, y1, y0));
+  }
 }
 
-__device__ __forceinline__ void tile_rot(double2* tile, int T, const Op& op) {
-  const double Tq = op.m[0], Sq = op.m[1];
-  const int t = op.target;
+template <bool FORM_B>
+__device__ __forceinline__ void tile_rot_form(double2* tile, int T, int t, double w) {
   const int half = T >> 1;
   const int bd = blockDim.x;
   for (int q = threadIdx.x; q < half; q += 2 * bd) {
@@ -345,16 +345,21 @@ __device__ __forceinline__ void tile_rot(double2* tile, int T, const Op& op) {
     if (q2 < half) {
       const uint32_t m0 = insert_zero32((uint32_t)q2, t), m1 = m0 | (1u << t);
       double2 b0 = tile[m0], b1 = tile[m1];
-      rot_pair(Tq, Sq, a0, a1);
-      rot_pair(Tq, Sq, b0, b1);
+      rot_pair<FORM_B>(w, a0, a1);
+      rot_pair<FORM_B>(w, b0, b1);
       tile[m0] = b0;
       tile[m1] = b1;
     } else {
-      rot_pair(Tq, Sq, a0, a1);
+      rot_pair<FORM_B>(w, a0, a1);
     }
     tile[l0] = a0;
     tile[l1] = a1;
   }
+}
+
+__device__ __forceinline__ void tile_rot(double2* tile, int T, const Op& op) {
+  if (op.m[1] == 0.0) tile_rot_form<false>(tile, T, op.target, op.m[0]);
+  else tile_rot_form<true>(tile, T, op.target, op.m[0]);
 }
 
 // OP_PHASE (FP64 window passes): amplitude l times the phase of table entry

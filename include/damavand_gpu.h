@@ -55,9 +55,11 @@ enum { DMV_C128 = 0, DMV_C64 = 1 };
  * The amplitudes are IEEE complex128 in device memory between calls in every mode.
  * DMV_ARITH_FP64: IEEE FP64 arithmetic (default). Fused window passes on the
  *   TMA kernel write each uncontrolled unitary 2x2 as diagonal x real rotation
- *   x diagonal, apply the rotation as three shears (3 FP64 multiply-adds per
- *   amplitude instead of 8) and collect the diagonals of a pass into a few
- *   per-amplitude phase tables, each applied with three more shears.
+ *   x diagonal, apply the rotation as a scaled matrix with one FP64
+ *   multiply-add per output (2 per amplitude instead of 8; the product of the
+ *   scale factors is multiplied back into the state once per forward) and
+ *   collect the diagonals of a pass into a few per-amplitude phase tables,
+ *   each applied with three shears (3 multiply-adds per amplitude).
  * DMV_ARITH_FP64_DIRECT: IEEE FP64 with every fused 2x2 applied as a full
  *   complex multiply-add (8 per amplitude for a general matrix).
  * The FP32-pair and int64 arithmetics below take the same rotation and phase
@@ -299,11 +301,14 @@ int dmv_debug_tc_convert(int32_t mode);
 /* Test hook: the number of polls after which a TMA window pass stops waiting
  * for a tile load (negative: the default). The pass then drains its copies,
  * leaves the state undefined and the next dmv_state_synchronize returns
- * DMV_ERR_TIMEOUT. No reference counterpart. */
+ * DMV_ERR_TIMEOUT. The same limit bounds the chunk-load waits of the
+ * bulk-staged readout passes (dmv_expect_z, dmv_sample, dmv_sample_expect_z
+ * from 12 qubits), which then return DMV_ERR_TIMEOUT themselves with
+ * undefined outputs; the state is unchanged. No reference counterpart. */
 int dmv_debug_tma_wait_limit(int64_t polls);
 /* Test hook (host only, no GPU): plans `gates` for num_qubits (12..34) with
  * 2^12-amplitude windows, rewrites every window pass into rotations and phase
- * tables in both forms (rotations as shears and tables by shears, as the FP64
+ * tables in both forms (scaled rotations and tables by shears, as the FP64
  * kernels apply them; rotations as real 2x2 ops and tables as complex values,
  * as the FP32-pair and int64 kernels do), applies the original and the
  * rewritten ops to two random tiles each in host FP64, and returns the
