@@ -227,6 +227,25 @@ void phase_tables_df(const std::vector<PhaseEntry>& in, std::vector<float4>& out
   }
 }
 
+void phase_tables_f64(const std::vector<PhaseEntry>& in, std::vector<double2>& out) {
+  out.resize(in.size());
+  for (size_t i = 0; i < in.size(); ++i) {
+    const PhaseEntry& e = in[i];
+    uint64_t tb, sb;
+    std::memcpy(&tb, &e.t, 8);
+    std::memcpy(&sb, &e.s, 8);
+    // |t| <= tan(pi/8), |s| <= sin(pi/4): bit 62 (the exponent's top bit) is 0
+    const uint64_t top = uint64_t(1) << 62;
+    const uint64_t q = (uint64_t)e.swap_xy | ((uint64_t)(e.sign_y != 0) << 1);
+    if (q & 1) tb |= top;
+    if (q & 2) sb |= top;
+    double t, sv;
+    std::memcpy(&t, &tb, 8);
+    std::memcpy(&sv, &sb, 8);
+    out[i] = make_double2(t, sv);
+  }
+}
+
 void phase_tables_fx(const std::vector<PhaseEntry>& in, std::vector<int4>& out) {
   out.resize(in.size());
   for (size_t i = 0; i < in.size(); ++i) {
@@ -425,8 +444,25 @@ struct Cx {
 
 // value_form: apply table entries as the complex value phase_entry_value gives
 // (the form the FP32-pair and int64 kernels read) instead of by shears.
+// The FP64 kernels' decode of a packed entry (phase_tables_f64): t, s and the
+// quadrant bits q & 1 (swap), q >> 1.
+void unpack_entry(const double2& p, double& t, double& s, int& b0, int& b1) {
+  uint64_t tb, sb;
+  std::memcpy(&tb, &p.x, 8);
+  std::memcpy(&sb, &p.y, 8);
+  const uint64_t top = uint64_t(1) << 62;
+  b0 = (int)((tb >> 62) & 1u);
+  b1 = (int)((sb >> 62) & 1u);
+  tb &= ~top;
+  sb &= ~top;
+  std::memcpy(&t, &tb, 8);
+  std::memcpy(&s, &sb, 8);
+}
+
+// value_form false: the table applied as the FP64 kernels do, from the packed
+// entries `packed` (phase_tables_f64 of `tab`).
 void host_op(std::vector<Cx>& tile, int k, const Op& op, const std::vector<PhaseEntry>& tab, uint64_t base,
-             bool value_form = false) {
+             bool value_form = false, const std::vector<double2>* packed = nullptr) {
   const uint32_t T = 1u << k;
   if (op.ctrl_kind == CTRL_GLOBAL && !((base >> op.ctrl) & 1u)) return;
   if (op.cls == OP_PHASE) {
@@ -441,12 +477,15 @@ void host_op(std::vector<Cx>& tile, int k, const Op& op, const std::vector<Phase
         tile[l] = Cx{re * v.re - im * v.im, re * v.im + im * v.re};
         continue;
       }
-      const double x1 = std::fma(e.t, v.im, v.re);
-      const double y1 = std::fma(e.s, x1, v.im);
-      const double x2 = std::fma(e.t, y1, x1);
-      double ox = e.swap_xy ? y1 : x2, oy = e.swap_xy ? x2 : y1;
-      if (e.sign_x) ox = -ox;
-      if (e.sign_y) oy = -oy;
+      double t = e.t, sv = e.s;
+      int b0 = (int)e.swap_xy, b1 = e.sign_y ? 1 : 0;
+      if (packed) unpack_entry((*packed)[(size_t)op.fh[0] + ((size_t)gsel << k) + l], t, sv, b0, b1);
+      const double x1 = std::fma(t, v.im, v.re);
+      const double y1 = std::fma(sv, x1, v.im);
+      const double x2 = std::fma(t, y1, x1);
+      double ox = b0 ? y1 : x2, oy = b0 ? x2 : y1;
+      if (b0 ^ b1) ox = -ox;  // sign_x: q = 1 or 2
+      if (b1) oy = -oy;       // sign_y: q = 2 or 3
       tile[l] = Cx{ox, oy};
     }
     return;
@@ -512,6 +551,8 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
     std::vector<PhaseEntry> tab;
     ScaleDD scale;
     rewrite_pass_rotations(plan.ops.data() + ps.op_begin, ps.op_count, k, form == 0, rw, tab, &scale);
+    std::vector<double2> packed;
+    phase_tables_f64(tab, packed);
     if (form == 0)
       for (const Op& o : rw) {
         n_rot += o.cls == OP_ROT;
@@ -532,7 +573,7 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
       // the original ops index controls outside the tile by global qubit; the host
       // emulation reads them from `base`, as the kernel does
       for (int64_t o = 0; o < ps.op_count; ++o) host_op(a, k, plan.ops[(size_t)(ps.op_begin + o)], tab, base);
-      for (const Op& o : rw) host_op(b, k, o, tab, base, form == 1);
+      for (const Op& o : rw) host_op(b, k, o, tab, base, form == 1, form == 0 ? &packed : nullptr);
       for (Cx& v : b) v = Cx{v.re * scale.hi, v.im * scale.hi};  // the rotations' factors
       double num = 0.0, den = 0.0;
       for (size_t i = 0; i < a.size(); ++i) {

@@ -191,6 +191,10 @@ void phase_entry_value(const PhaseEntry& e, double& re, double& im);
 // The tables in the FP32-pair form (re_h, re_l, im_h, im_l) and as Q.54 limbs
 // (re_h, re_l, im_h, im_l: value = h * 2^31 + l, l in [0, 2^31)).
 void phase_tables_df(const std::vector<PhaseEntry>& in, std::vector<float4>& out);
+// The FP64 kernels' 16-byte form: (t, s) with the quadrant in bit 62 of each
+// (0 in both, as |t|, |s| < 2): bit 62 of t = swap_xy = q & 1, bit 62 of s =
+// q >> 1 (sign_y); sign_x = the xor of the two.
+void phase_tables_f64(const std::vector<PhaseEntry>& in, std::vector<double2>& out);
 void phase_tables_fx(const std::vector<PhaseEntry>& in, std::vector<int4>& out);
 
 // Arithmetic used for complex128 storage.
@@ -337,6 +341,7 @@ struct dmv_state_s {
   std::vector<dmv::PhaseEntry> phase_tab;  // phase tables of the rewritten passes
   std::vector<dmv::ScaleDD> pass_scale;  // launch_plan: OP_ROT factor product per staged pass
   dmv::DeviceBuffer phase_tab_dev;
+  std::vector<double2> phase_tab_f64;      // the tables in the FP64 kernels' 16-byte form
   std::vector<float4> phase_tab_df;        // the same tables for the FP32-pair arithmetic
   std::vector<int4> phase_tab_fx;          // and for the int64 arithmetic
   dmv::DeviceBuffer phase_tab2_dev;

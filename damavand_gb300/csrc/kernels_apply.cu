@@ -253,7 +253,7 @@ struct TmaPassParams {
   int64_t num_tiles;
   const Op* ops;
   const PhaseOp* phase_ops;  // k_window_phases' op table (num_ops <= kMaxPhaseOps)
-  const void* phase_tab;  // k_window_tma: tables of the pass's OP_PHASE ops (PhaseEntry)
+  const void* phase_tab;  // k_window_tma: tables of the pass's OP_PHASE ops (the policy's form)
   void* amps;        // the statevector (k_window_tma's thread stores)
   int* status;       // set to 1 when a wait gave up
 };
@@ -742,9 +742,10 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   const void* phase_tab2_dev = nullptr;
   int64_t tab2_bytes = 0;
   if (!s->phase_tab.empty()) {
-    DMV_TRY(s->phase_tab_dev.reserve(s->phase_tab.size() * sizeof(PhaseEntry)));
-    DMV_CUDA_TRY(cudaMemcpyAsync(s->phase_tab_dev.ptr, s->phase_tab.data(), s->phase_tab.size() * sizeof(PhaseEntry),
-                                 cudaMemcpyHostToDevice, s->stream));
+    phase_tables_f64(s->phase_tab, s->phase_tab_f64);
+    DMV_TRY(s->phase_tab_dev.reserve(s->phase_tab_f64.size() * sizeof(double2)));
+    DMV_CUDA_TRY(cudaMemcpyAsync(s->phase_tab_dev.ptr, s->phase_tab_f64.data(),
+                                 s->phase_tab_f64.size() * sizeof(double2), cudaMemcpyHostToDevice, s->stream));
     phase_tab_dev = s->phase_tab_dev.ptr;
     const void* src2 = nullptr;
     if (s->arith == ARITH_FP32X2) {
@@ -875,7 +876,7 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
     }
   s->last_passes = (int64_t)passes.size();
   s->last_ops = (int64_t)plan.ops.size();
-  s->last_phase_tab_bytes = (int64_t)(s->phase_tab.size() * sizeof(PhaseEntry));
+  s->last_phase_tab_bytes = (int64_t)(s->phase_tab_f64.size() * sizeof(double2));
   s->last_upload_bytes = s->last_phase_tab_bytes + tab2_bytes + (any_window ? (int64_t)(ops.size() * sizeof(Op)) : 0) +
                          (any_phases ? (int64_t)(s->phase_ops.size() * sizeof(PhaseOp)) : 0) +
                          (tc ? (int64_t)(s->tc_stages.size() * sizeof(TcStage) + s->tc_u.size() * 2) : 0);

@@ -363,26 +363,30 @@ __device__ __forceinline__ void tile_rot(double2* tile, int T, const Op& op) {
 }
 
 // OP_PHASE (FP64 window passes): amplitude l times the phase of table entry
-// op.fh[0] + (gsel << k) + l (PhaseEntry: three shears, then a swap and sign
-// flips for the factor i^q on the integer pipe). gsel holds the tile's bits at
-// the op.fh[1] global qubits op.fh[2..].
-__device__ __forceinline__ void tile_phase(double2* tile, int T, const Op& op, const PhaseEntry* tab, int64_t base) {
+// op.fh[0] + (gsel << k) + l, in the 16-byte form of phase_tables_f64: three
+// shears by (t, s), then for the factor i^q a swap and sign flips on the
+// integer pipe, q read from bit 62 of t (q & 1: swap) and of s (q >> 1).
+// gsel holds the tile's bits at the op.fh[1] global qubits op.fh[2..].
+__device__ __forceinline__ void tile_phase(double2* tile, int T, const Op& op, const double2* tab, int64_t base) {
   const int k = 31 - __clz(T);
   int gsel = 0;
   for (int j = 0; j < op.fh[1]; ++j) gsel |= (int)((base >> op.fh[2 + j]) & 1) << j;
-  const PhaseEntry* e = tab + op.fh[0] + ((int64_t)gsel << k);
+  const double2* e = tab + op.fh[0] + ((int64_t)gsel << k);
 #pragma unroll 4
   for (int l = threadIdx.x; l < T; l += blockDim.x) {
-    const double2 ts = __ldg(reinterpret_cast<const double2*>(e + l));
-    const uint4 fl = __ldg(reinterpret_cast<const uint4*>(e + l) + 1);
+    const double2 ts = __ldg(e + l);
+    const int th = __double2hiint(ts.x), sh = __double2hiint(ts.y);
+    const int b0 = (th >> 30) & 1, b1 = (sh >> 30) & 1;
+    const double t = __hiloint2double(th & ~(1 << 30), __double2loint(ts.x));
+    const double s = __hiloint2double(sh & ~(1 << 30), __double2loint(ts.y));
     const double2 v = tile[l];
-    const double x1 = fma(ts.x, v.y, v.x);
-    const double y1 = fma(ts.y, x1, v.y);
-    const double x2 = fma(ts.x, y1, x1);
-    const double ox = fl.x ? y1 : x2;
-    const double oy = fl.x ? x2 : y1;
-    tile[l] = make_double2(__hiloint2double(__double2hiint(ox) ^ (int)fl.y, __double2loint(ox)),
-                           __hiloint2double(__double2hiint(oy) ^ (int)fl.z, __double2loint(oy)));
+    const double x1 = fma(t, v.y, v.x);
+    const double y1 = fma(s, x1, v.y);
+    const double x2 = fma(t, y1, x1);
+    const double ox = b0 ? y1 : x2;
+    const double oy = b0 ? x2 : y1;
+    tile[l] = make_double2(__hiloint2double(__double2hiint(ox) ^ ((b0 ^ b1) << 31), __double2loint(ox)),
+                           __hiloint2double(__double2hiint(oy) ^ (b1 << 31), __double2loint(oy)));
   }
 }
 
@@ -438,7 +442,7 @@ __device__ __forceinline__ void tile_phase_fx(longlong2* tile, int T, const Op& 
 // Every op of a pass on one tile; `base` holds the tile's global index bits
 // (controls outside the tile are read from it). Ends with a barrier after
 // each applied op. `tab` holds the phase tables of OP_PHASE ops in the
-// policy's form: PhaseEntry (FP64), float4 FP32 pairs (PolDF) or int4 Q.54
+// policy's form: 16-byte packed entries (FP64, phase_tables_f64), float4 FP32 pairs (PolDF) or int4 Q.54
 // limbs (PolFX).
 template <typename P>
 __device__ __forceinline__ void tile_apply_ops(typename P::T* tile, int T, const Op* ops, int num_ops, int64_t base,
@@ -453,7 +457,7 @@ __device__ __forceinline__ void tile_apply_ops(typename P::T* tile, int T, const
         continue;
       }
       if (op.cls == OP_PHASE) {
-        tile_phase(tile, T, op, static_cast<const PhaseEntry*>(tab), base);
+        tile_phase(tile, T, op, static_cast<const double2*>(tab), base);
         __syncthreads();
         continue;
       }
