@@ -60,11 +60,11 @@ FP32_FMA_PEAK_T = 35.9
 # dram__bytes_read.sum + dram__bytes_write.sum per launch divided by the amplitudes of
 # the captured case: one ncu capture per kernel on a smaller state of the same ladder
 # workload (dram__bytes.sum.per_second x gpu__time_duration.sum: k_window_tma<PolF64>
-# 480.0 MB at 2^24 amplitudes; k_window_phases<PolF32> 1012.4 MB at 2^26; k_window_tc
+# 479.1 MB at 2^24 amplitudes; k_window_phases<PolF32> 1012.4 MB at 2^26; k_window_tc
 # 476.1 MB at 2^24; k_apply_window<PolDF> 492.7 MB and k_apply_window<PolFX> 493.1 MB at
 # 2^24). Traffic is the state read plus written once per pass, so it scales with the
 # number of amplitudes.
-NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 479.998720e6 / (1 << 24),
+NCU_TRAFFIC_PER_AMPLITUDE = {("window", "c128"): 479.1e6 / (1 << 24),
                              ("window", "c64"): 1012.4e6 / (1 << 26),
                              ("window", "c128", "tc"): 476.1e6 / (1 << 24),
                              ("window", "c128", "fp32x2"): 492.7e6 / (1 << 24),
