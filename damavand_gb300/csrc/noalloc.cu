@@ -13,10 +13,10 @@
 // use the array's name as an address (on the host it is only a stand-in), so
 // the first call on each device looks its device address up with
 // cudaGetSymbolAddress, with that device current, and caches it. That first
-// call may also load the library's device code onto the device; make it before
-// any stream capture. All calls share the one array: calls whose kernels
-// overlap on the GPU (different streams, or different host threads on one
-// device) race on it and must be serialised by the caller.
+// call may also load the library's device code onto the device. All calls
+// share the one array: calls whose kernels overlap on the GPU (different
+// streams, or different host threads on one device) race on it and must be
+// serialised by the caller.
 #include <mutex>
 
 #include "complex_ops.cuh"

@@ -246,9 +246,9 @@ int dmv_inner_product(dmv_state_t a, dmv_state_t b, double* re, double* im);
  * compiled into the library (1216 x 35 doubles, 332.5 KiB, held on every GPU
  * that loads the library until exit), hence num_qubits <= 34; larger sizes
  * are rejected with DMV_ERR_INVALID. The first call on each device looks the
- * array's device address up (and may load the library's device code): make
- * it before any stream capture. Every call shares the array, so calls whose
- * kernels overlap on the GPU race; serialise them. */
+ * array's device address up (and may load the library's device code). Every
+ * call shares the array, so calls whose kernels overlap on the GPU race;
+ * serialise them. */
 int dmv_expect_z_noalloc(const void* amps, int32_t num_qubits, int32_t precision, double* out_device,
                          void* stream);
 
