@@ -101,6 +101,7 @@ SIGNATURES = {
     "dmv_debug_tma_wait_limit": (ctypes.c_int, [_i64]),
     "dmv_debug_tc_convert": (ctypes.c_int, [_i32]),
     "dmv_debug_check_fp64_rewrite": (ctypes.c_int, [ctypes.c_void_p, _i64, _i32, ctypes.c_uint64, _dp, _i64p]),
+    "dmv_debug_adjoint_plan": (ctypes.c_int, [ctypes.c_void_p, _i64, _i32, _i64p]),
     "dmv_circuit_create": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, _vpp]),
     "dmv_circuit_destroy": (ctypes.c_int, [_vp]),
     "dmv_circuit_add_gate": (ctypes.c_int, [_vp, _i32, _i32, _i32, _f64, _i32]),

@@ -382,4 +382,59 @@ int64_t assign_phases(Op* ops, int64_t count, int32_t tile_bits, int32_t rb) {
   return phases;
 }
 
+int build_adjoint_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision, const PlanOptions& base,
+                       Plan& plan) {
+  std::vector<Gate> rev;
+  std::vector<int32_t> param, gen;
+  int32_t slots = 0;
+  for (const Gate& g : gates)
+    if (!g.observable && is_parametrised(g.kind)) ++slots;
+  rev.reserve(gates.size());
+  for (int64_t gi = (int64_t)gates.size() - 1; gi >= 0; --gi) {
+    const Gate& g = gates[(size_t)gi];
+    if (g.observable) continue;
+    Gate h = g;
+    adjoint2(g.m, h.m);
+    rev.push_back(h);
+    const bool p = is_parametrised(g.kind);
+    if (p) --slots;  // slots now the list-order index of this gate's parameter
+    param.push_back(p ? slots : -1);
+    gen.push_back(p ? rotation_generator(g.kind) : 0);
+  }
+  PlanOptions opt = base;
+  opt.param_of = param.data();
+  opt.generator_of = gen.data();
+  return build_plan(rev, n, precision, opt, plan);
+}
+
 }  // namespace dmv
+
+extern "C" int dmv_debug_adjoint_plan(const dmv_gate_t* gates, int64_t num_gates, int32_t num_qubits,
+                                      int64_t* counts) {
+  using namespace dmv;
+  clear_error();
+  if (!counts) return set_error(DMV_ERR_INVALID, "dmv_debug_adjoint_plan: null counts");
+  std::vector<Gate> g;
+  DMV_TRY(parse_gates(gates, num_gates, num_qubits, g));
+  PlanOptions opt;
+  opt.fusion = DMV_FUSE_WINDOW;
+  opt.tile_bits = 12;
+  Plan plan;
+  DMV_TRY(build_adjoint_plan(g, num_qubits, DMV_C128, opt, plan));
+  int64_t windows = 0, tagged = 0, max_param = -1, mismatched = 0;
+  for (const Pass& ps : plan.passes) windows += ps.kind == 1;
+  for (const Op& op : plan.ops) {
+    if (op.param >= 0) {
+      ++tagged;
+      max_param = std::max<int64_t>(max_param, op.param);
+    }
+    if ((op.param >= 0) != (op.generator != 0)) ++mismatched;
+  }
+  counts[0] = (int64_t)plan.passes.size();
+  counts[1] = windows;
+  counts[2] = (int64_t)plan.ops.size();
+  counts[3] = tagged;
+  counts[4] = max_param + 1;
+  counts[5] = mismatched;
+  return DMV_OK;
+}

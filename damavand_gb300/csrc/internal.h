@@ -260,6 +260,12 @@ struct PlanOptions {
 
 int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
                const PlanOptions& opt, Plan& plan);
+// The reverse sweep of an adjoint gradient as a plan: the non-observable gates
+// in reverse order, each replaced by U^dagger, unmerged, each op tagged with
+// its gate's parameter slot (list order of the parametrised gates) and
+// generator (PlanOptions::param_of / generator_of).
+int build_adjoint_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision, const PlanOptions& base,
+                       Plan& plan);
 
 // ---------------------------------------------------------------------------
 // Tensor-core window passes (ARITH_TC, complex128 storage).

@@ -1472,28 +1472,12 @@ int launch_adjoint_step_impl(dmv_state_s* psi, dmv_state_s* lam, const Op& op, i
 }
 
 // The reverse sweep over psi and lam in the FP32-pair form, fused into
-// windows: the gate list reversed, each gate replaced by U^dagger and tagged
-// with its parameter slot and generator, planned without merging; window
-// passes run k_adjoint_window, single-gate passes k_adjoint_step.
+// windows (build_adjoint_plan): window passes run k_adjoint_window,
+// single-gate passes k_adjoint_step.
 int adjoint_sweep_windows(dmv_state_s* s, dmv_state_s* psi, dmv_state_s* lam, const std::vector<Gate>& gates,
-                          const std::vector<int64_t>& slot_of, double* part, int64_t cols, DeviceBuffer& ops_buf) {
-  std::vector<Gate> rev;
-  std::vector<int32_t> param, gen;
-  rev.reserve(gates.size());
-  for (int64_t gi = (int64_t)gates.size() - 1; gi >= 0; --gi) {
-    const Gate& g = gates[(size_t)gi];
-    if (g.observable) continue;
-    Gate h = g;
-    adjoint2(g.m, h.m);
-    rev.push_back(h);
-    param.push_back((int32_t)slot_of[(size_t)gi]);
-    gen.push_back(slot_of[(size_t)gi] >= 0 ? rotation_generator(g.kind) : 0);
-  }
-  PlanOptions opt = plan_options_for(s, DMV_FUSE_WINDOW);
-  opt.param_of = param.data();
-  opt.generator_of = gen.data();
+                          double* part, int64_t cols, DeviceBuffer& ops_buf) {
   Plan plan;
-  DMV_TRY(build_plan(rev, s->n, s->precision, opt, plan));
+  DMV_TRY(build_adjoint_plan(gates, s->n, s->precision, plan_options_for(s, DMV_FUSE_WINDOW), plan));
   if (!plan.ops.empty()) {
     DMV_TRY(ops_buf.reserve(plan.ops.size() * sizeof(Op)));
     DMV_CUDA_TRY(cudaMemcpyAsync(ops_buf.ptr, plan.ops.data(), plan.ops.size() * sizeof(Op), cudaMemcpyHostToDevice,
@@ -1569,7 +1553,7 @@ int adjoint_gradient(dmv_state_s* s, const std::vector<Gate>& gates, const doubl
       count_launch(2);
     }
     if (df_raw) {
-      rc = adjoint_sweep_windows(s, psi, lam, gates, slot_of, part, grid, adj_ops);
+      rc = adjoint_sweep_windows(s, psi, lam, gates, part, grid, adj_ops);
       if (rc != DMV_OK) break;
     }
     for (int64_t gi = df_raw ? -1 : (int64_t)gates.size() - 1; gi >= 0 && rc == DMV_OK; --gi) {

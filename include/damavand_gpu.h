@@ -317,6 +317,13 @@ int dmv_debug_tma_wait_limit(int64_t polls);
  * reference counterpart. */
 int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num_gates, int32_t num_qubits, uint64_t seed,
                                  double* max_err, int64_t* counts);
+/* Test hook (host only, no GPU): plans the reverse sweep of an adjoint
+ * gradient over `gates` (reversed, each gate's adjoint, unmerged, ops tagged
+ * with parameter slots and generators, 2^12-amplitude windows) and writes 6
+ * counts: passes, window passes, ops, tagged ops, the largest slot + 1, and
+ * ops whose slot and generator disagree (one set, the other not). No
+ * reference counterpart. */
+int dmv_debug_adjoint_plan(const dmv_gate_t* gates, int64_t num_gates, int32_t num_qubits, int64_t* counts);
 
 /* ------------------------------------------------------------------------ */
 /* Circuit front-end (the reference's pyo3 Circuit, src/qubit_backend/circuit.rs:78-770) */

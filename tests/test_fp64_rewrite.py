@@ -99,3 +99,28 @@ def test_rewrite_with_controlled_phases_and_matrices(built_lib):
     assert lib.dmv_debug_check_fp64_rewrite(ctypes.cast(arr, ctypes.c_void_p), len(gates), n, 3,
                                             ctypes.byref(err), counts) == 0, lib.dmv_last_error_string()
     assert err.value < 1e-13, err.value
+
+
+def _adjoint_plan(lib, n, gates):
+    from damavand_gb300.workloads import gate_array
+    arr, count = gate_array(gates)
+    counts = (ctypes.c_int64 * 6)()
+    rc = lib.dmv_debug_adjoint_plan(ctypes.cast(arr, ctypes.c_void_p), count, n, counts)
+    assert rc == 0, lib.dmv_last_error_string()
+    return list(counts)
+
+
+@pytest.mark.parametrize("n,controlled", [(10, False), (16, True), (24, False)])
+def test_adjoint_sweep_plan_keeps_every_gate_and_tags_each_parameter(built_lib, n, controlled):
+    """The reverse sweep's plan (host only): no gate merged, one op per non-observable
+    gate, each parametrised gate's op tagged with its own slot and generator, windows
+    formed."""
+    from damavand_gb300.workloads import PARAMETRISED, random_circuit, ring_ansatz
+    rng = np.random.default_rng(90 + n)
+    gates = ring_ansatz(n, 3, seed=n) + random_circuit(n, 4, rng, controlled_rotations=controlled)
+    gates.append((3, 1, -1, True, 0.0))  # an observable: skipped
+    passes, windows, ops, tagged, slots, mismatched = _adjoint_plan(built_lib.lib, n, gates)
+    params = sum(1 for k, _, _, obs, _ in gates if k in PARAMETRISED and not obs)
+    assert ops == len(gates) - 1
+    assert tagged == params and slots == params and mismatched == 0
+    assert windows > 0 and passes >= windows

@@ -17,11 +17,18 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _torchrun(args, timeout=300):
-    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
-           "--master-addr", "127.0.0.1", "--master-port", str(_free_port())] + args
+def _torchrun(args, timeout=300, attempts=2):
+    """Two ranks under torchrun on 127.0.0.1. A launch that fails is retried once on
+    a fresh port: the port is picked before torchrun binds it, so another process
+    can take it in between; a real failure fails both times."""
     env = dict(os.environ, OMP_NUM_THREADS="2")
-    return subprocess.run(cmd, cwd=REPO, capture_output=True, text=True, timeout=timeout, env=env)
+    for _ in range(attempts):
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+               "--master-addr", "127.0.0.1", "--master-port", str(_free_port())] + args
+        res = subprocess.run(cmd, cwd=REPO, capture_output=True, text=True, timeout=timeout, env=env)
+        if res.returncode == 0:
+            break
+    return res
 
 
 def test_replica_barrier_and_max_over_ranks():
