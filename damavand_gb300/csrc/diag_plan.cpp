@@ -266,6 +266,7 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool rot
   uint32_t touched = 0;   // target bits of the ops emitted after `last` (after the pass start if none)
   DiagTable pend;
   pend.reset(T);
+  ScaleDD acc;  // OP_ROT factors not yet in the state (rot_ops)
 
   auto flush = [&]() {
     if (!pend.used) return;
@@ -341,13 +342,30 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool rot
           // component instead of three shears; f (>= 1/sqrt 2) goes to *scale.
           // f = 1 / sqrt(1 + w^2), rounded once from a wider result, so that
           // f M is orthogonal to within that rounding (no norm drift).
+          // The factors left out since the last fold live in `acc`; before
+          // the stored values could grow past 2^200 this rotation is applied
+          // as the real 2x2 acc f M instead (8 multiply-adds per pair), which
+          // gives the state its true scale back.
           (void)Tq;
-          r.cls = OP_ROT;
-          const double w = Cq >= Sq ? Sq / Cq : Cq / Sq;
-          r.m[0] = w;
-          r.m[1] = Cq >= Sq ? 0.0 : 1.0;
+          const bool form_b = Cq < Sq;
+          const double w = form_b ? Cq / Sq : Sq / Cq;
           const long double wl = w;
-          if (scale) scale->mul((double)(1.0L / std::sqrt(1.0L + wl * wl)));
+          const double f = (double)(1.0L / std::sqrt(1.0L + wl * wl));
+          if (acc.hi * f >= 0x1p-200) {
+            r.cls = OP_ROT;
+            r.m[0] = w;
+            r.m[1] = form_b ? 1.0 : 0.0;
+            acc.mul(f);
+          } else {
+            const long double F = ((long double)acc.hi + (long double)acc.lo) * (long double)f;
+            const double one = (double)F, ww = (double)(F * wl);
+            r.cls = OP_REAL;
+            r.m[0] = form_b ? ww : one;
+            r.m[2] = form_b ? -one : -ww;
+            r.m[4] = form_b ? one : ww;
+            r.m[6] = form_b ? ww : one;
+            acc = ScaleDD();
+          }
         } else {  // the rotation as a real 2x2 in the arithmetic's own form
           r.cls = OP_REAL;
           r.m[0] = Cq;
@@ -426,6 +444,7 @@ int64_t rewrite_pass_rotations(const Op* src, int64_t count, int32_t k, bool rot
     if (it.flush) put_table(tables[(size_t)it.table]);
     else dst.push_back(it.op);
   }
+  if (scale) scale->mul(acc);
   return (int64_t)dst.size() - before;
 }
 
@@ -580,7 +599,8 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
         num = std::max(num, std::hypot(a[i].re - b[i].re, a[i].im - b[i].im));
         den = std::max(den, std::hypot(a[i].re, a[i].im));
       }
-      worst = std::max(worst, den > 0 ? num / den : num);
+      const double e = den > 0 ? num / den : num;
+      worst = std::isfinite(e) ? std::max(worst, e) : INFINITY;  // NaN must not pass as 0
     }
     }
   }

@@ -801,14 +801,15 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   // the FP32-pair form between them (k_apply_window's FMT bits).
   bool df_chain = c128 && s->arith == ARITH_FP32X2 && passes.size() >= 2;
   for (const Pass& ps : passes) df_chain = df_chain && ps.kind == 1;
-  // The OP_ROT factors left out of the state so far (each in [1/sqrt 2, 1]):
-  // multiplied back at the end, or earlier before the stored values could
-  // grow past 2^300.
+  // The OP_ROT factors left out of the state so far (each in [1/sqrt 2, 1];
+  // a pass leaves at most 2^200 out, rewrite_pass_rotations folds the rest
+  // back itself): multiplied back at the end, or after a pass when the stored
+  // values could have grown past 2^200.
   ScaleDD owed;
   for (size_t pi = 0; pi < passes.size(); ++pi) {
     if (pi > 0) {
       owed.mul(pass_scale[pi - 1]);
-      if (std::fabs(owed.hi) < 0x1p-300) {
+      if (std::fabs(owed.hi) < 0x1p-200) {
         DMV_TRY(launch_scale_state(s, owed.hi));
         owed = ScaleDD();
       }

@@ -124,3 +124,13 @@ def test_adjoint_sweep_plan_keeps_every_gate_and_tags_each_parameter(built_lib, 
     assert ops == len(gates) - 1
     assert tagged == params and slots == params and mismatched == 0
     assert windows > 0 and passes >= windows
+
+
+def test_rewrite_of_a_deep_single_pass(built_lib):
+    """12 qubits, 1000 ladder layers: one window pass with 12000 rotations, whose
+    factors (each >= 1/sqrt 2) would leave the FP64 range; the rewrite folds them back
+    (a handful of rotations applied as full real 2x2 ops) and the check stays finite."""
+    from damavand_gb300.workloads import ladder_circuit
+    err, (passes, general, rot, phase) = _check(built_lib.lib, 12, ladder_circuit(12, 1000, seed=3))
+    assert math.isfinite(err) and err < 1e-13, err
+    assert passes == 1 and general == 12000 and 11900 < rot < 12000

@@ -1,4 +1,5 @@
-"""GPU: the FP64 window passes as rotations (three shears) and phase tables
+"""GPU: the FP64 window passes as rotations (one multiply-add per output, the
+factors multiplied back) and phase tables
 (DMV_ARITH_FP64, the default) against the oracle and against the same
 passes applied as full complex 2x2 multiply-adds (DMV_ARITH_FP64_DIRECT):
 every gate kind, exchanges controlled from outside the tile, controlled
@@ -33,6 +34,22 @@ def test_random_circuits_against_oracle(built_lib, oracle_mod, n, seed):
     err = np.max(np.abs(c.state_numpy() - want)) / np.max(np.abs(want))
     assert err <= AMP_RTOL, err
     assert np.max(np.abs(c.expectation_z() - oracle_mod.expect_z(oracle_mod.measure(want)))) <= EXPECT_ATOL
+
+
+@pytest.mark.parametrize("n,layers", [(12, 600), (16, 150)])
+def test_deep_passes_keep_the_state_scale(built_lib, oracle_mod, n, layers):
+    """Thousands of rotations in one window pass (12 qubits: the whole circuit is one
+    pass) or a few passes: the factors left out of the state are folded back inside the
+    pass and between passes, so the stored values never leave FP64's range."""
+    from damavand_gb300.workloads import ladder_circuit
+    gates = ladder_circuit(n, layers, seed=9)
+    want = oracle_mod.forward(n, [(k, t, c, int(o), th) for k, t, c, o, th in gates], clone=False)
+    c = _run(n, gates, "fp64")
+    got = c.state_numpy()
+    assert np.all(np.isfinite(got))
+    err = np.max(np.abs(got - want)) / np.max(np.abs(want))
+    assert err <= AMP_RTOL, err
+    assert abs(c.norm() - 1.0) < 1e-12
 
 
 def test_ladder_26_qubits_rewritten_equals_direct(built_lib):
