@@ -39,6 +39,8 @@
 #include <cmath>
 #include <algorithm>
 #include <cstring>
+#include <atomic>
+#include <thread>
 
 #include "internal.h"
 
@@ -225,6 +227,30 @@ void phase_tables_df(const std::vector<PhaseEntry>& in, std::vector<float4>& out
     const float rh = (float)re, ih = (float)im;
     out[i] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
   }
+}
+
+void rewrite_passes(const Plan& plan, const std::vector<int64_t>& which, bool rot_ops,
+                    std::vector<RewrittenPass>& out) {
+  out.assign(which.size(), RewrittenPass());
+  auto work = [&](size_t j) {
+    const Pass& ps = plan.passes[(size_t)which[j]];
+    rewrite_pass_rotations(plan.ops.data() + ps.op_begin, ps.op_count, ps.low_bits + ps.num_high, rot_ops,
+                           out[j].ops, out[j].tab, &out[j].scale);
+  };
+  const size_t nt = std::min<size_t>(std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 16),
+                                     which.size());
+  if (nt <= 1) {
+    for (size_t j = 0; j < which.size(); ++j) work(j);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  pool.reserve(nt);
+  for (size_t t = 0; t < nt; ++t)
+    pool.emplace_back([&]() {
+      for (size_t j = next.fetch_add(1); j < which.size(); j = next.fetch_add(1)) work(j);
+    });
+  for (std::thread& th : pool) th.join();
 }
 
 void phase_tables_f64(const std::vector<PhaseEntry>& in, std::vector<double2>& out) {
@@ -560,9 +586,30 @@ extern "C" int dmv_debug_check_fp64_rewrite(const dmv_gate_t* gates, int64_t num
   };
   double worst = 0.0;
   int64_t n_rot = 0, n_phase = 0, n_general = 0, n_passes = 0;
+  // the threaded rewrite (what launch_plan runs) must give every pass exactly
+  // the sequential result
+  std::vector<int64_t> which;
+  for (size_t i = 0; i < plan.passes.size(); ++i)
+    if (plan.passes[i].kind == 1) which.push_back((int64_t)i);
+  std::vector<RewrittenPass> threaded[2];
+  rewrite_passes(plan, which, true, threaded[0]);
+  rewrite_passes(plan, which, false, threaded[1]);
+  size_t wi = 0;
   for (const Pass& ps : plan.passes) {
     if (ps.kind != 1) continue;
+    const size_t j = wi++;
     const int k = ps.low_bits + ps.num_high;
+    for (int form = 0; form < 2; ++form) {
+      std::vector<Op> rw;
+      std::vector<PhaseEntry> tab;
+      ScaleDD scale;
+      rewrite_pass_rotations(plan.ops.data() + ps.op_begin, ps.op_count, k, form == 0, rw, tab, &scale);
+      const RewrittenPass& t = threaded[form][j];
+      if (t.ops.size() != rw.size() || t.tab.size() != tab.size() || t.scale.hi != scale.hi ||
+          t.scale.lo != scale.lo || (!rw.empty() && std::memcmp(t.ops.data(), rw.data(), rw.size() * sizeof(Op))) ||
+          (!tab.empty() && std::memcmp(t.tab.data(), tab.data(), tab.size() * sizeof(PhaseEntry))))
+        return set_error(DMV_ERR_INVALID, "threaded rewrite of pass %zu differs from the sequential one", j);
+    }
     if (k != 12 || ps.num_high < 3) continue;
     ++n_passes;
     for (int form = 0; form < 2; ++form) {  // rotations as OP_ROT (FP64), then as real 2x2 ops

@@ -266,6 +266,16 @@ int build_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision,
 // generator (PlanOptions::param_of / generator_of).
 int build_adjoint_plan(const std::vector<Gate>& gates, int32_t n, int32_t precision, const PlanOptions& base,
                        Plan& plan);
+// rewrite_pass_rotations of several window passes, on host threads: pass
+// which[j] of `plan` into out[j] (its own ops, its own tables with OP_PHASE
+// offsets from 0, its factor product). Results do not depend on the threads.
+struct RewrittenPass {
+  std::vector<Op> ops;
+  std::vector<PhaseEntry> tab;
+  ScaleDD scale;
+};
+void rewrite_passes(const Plan& plan, const std::vector<int64_t>& which, bool rot_ops,
+                    std::vector<RewrittenPass>& out);
 
 // ---------------------------------------------------------------------------
 // Tensor-core window passes (ARITH_TC, complex128 storage).

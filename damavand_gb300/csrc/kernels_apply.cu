@@ -688,18 +688,36 @@ int launch_plan(dmv_state_s* s, const Plan& plan) {
   // Per staged pass, the product of its OP_ROT factors (1 elsewhere).
   std::vector<ScaleDD>& pass_scale = s->pass_scale;
   pass_scale.clear();
-  for (const Pass& ps : plan.passes) {
+  // The window passes' rewrites run on host threads (each pass independent);
+  // their tables are appended in pass order with the OP_PHASE offsets moved.
+  std::vector<RewrittenPass> rewritten;
+  std::vector<int64_t> rewritten_at(plan.passes.size(), -1);
+  if (rewrite) {
+    std::vector<int64_t> which;
+    for (size_t i = 0; i < plan.passes.size(); ++i)
+      if (plan.passes[i].kind == 1) {
+        rewritten_at[i] = (int64_t)which.size();
+        which.push_back((int64_t)i);
+      }
+    rewrite_passes(plan, which, rot_ops, rewritten);
+  }
+  for (size_t pi = 0; pi < plan.passes.size(); ++pi) {
+    const Pass& ps = plan.passes[pi];
     const int rb = ps.kind == 1 ? window_reg_bits(s, ps) : 0;
     any_window |= ps.kind == 1;
-    if (rewrite && ps.kind == 1) {
+    if (rewritten_at[pi] >= 0) {
+      const RewrittenPass& r = rewritten[(size_t)rewritten_at[pi]];
       Pass rw = ps;
       rw.op_begin = (int64_t)ops.size();
-      std::vector<Op> src(plan.ops.begin() + ps.op_begin, plan.ops.begin() + ps.op_begin + ps.op_count);
-      ScaleDD f;
-      rw.op_count =
-          rewrite_pass_rotations(src.data(), ps.op_count, ps.low_bits + ps.num_high, rot_ops, ops, s->phase_tab, &f);
+      rw.op_count = (int64_t)r.ops.size();
+      const int32_t tab_base = (int32_t)s->phase_tab.size();
+      for (Op op : r.ops) {
+        if (op.cls == OP_PHASE) op.fh[0] += tab_base;
+        ops.push_back(op);
+      }
+      s->phase_tab.insert(s->phase_tab.end(), r.tab.begin(), r.tab.end());
       passes.push_back(rw);
-      pass_scale.push_back(f);
+      pass_scale.push_back(r.scale);
       continue;
     }
     if (rb <= 0) {
