@@ -134,3 +134,15 @@ def test_rewrite_of_a_deep_single_pass(built_lib):
     err, (passes, general, rot, phase) = _check(built_lib.lib, 12, ladder_circuit(12, 1000, seed=3))
     assert math.isfinite(err) and err < 1e-13, err
     assert passes == 1 and general == 12000 and 11900 < rot < 12000
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_rewrite_with_controlled_rotations(built_lib, seed):
+    """Controlled rotations (local and outside-tile controls) stay general 2x2 ops; the
+    rewrite of the passes around them still matches the direct ops."""
+    from damavand_gb300.workloads import random_circuit
+    rng = np.random.default_rng(300 + seed)
+    n = int(rng.integers(14, 20))
+    err, counts = _check(built_lib.lib, n, random_circuit(n, 10, rng, controlled_rotations=True), seed=seed)
+    assert math.isfinite(err) and err < 1e-14, err
+    assert counts[0] > 0
